@@ -1,0 +1,423 @@
+#!/usr/bin/env python
+"""Benchmark of the FLUE hot path on GB300: 5-loop F_munu + B^2 forward +
+backward (the su(3) gradient of B^2) on a 32^3 x 64 lattice.
+
+One "step" = one call of flue_magnetic_force on a device-resident FP32 field
+(reconstruct-12 by default): lines -> F and B^2 -> line cotangents -> link
+gradient.  ``value`` is sites/s = n_ranks * V / (max over ranks of the
+device time per step).  The same step in FP64 (complex128), the FP32 error
+against FP64, the end-to-end call through the host-buffer C ABI
+(flue_magnetic_force_c: H2D of the field, kernels, D2H of the gradient) and
+the CPU baseline (the oracle's OpenMP restatement of the reference's
+magnetic(), forward only -- the reference has no backward) are reported on
+the same JSON line.
+
+Synthetic data: links exp(i eps H), H = sum_a c_a lambda_a / 2, c_a ~ N(0,1)
+from numpy PCG64(seed), eps = 0.3, reunitarised (FixSU3Matrix).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Multi-GPU (torchrun): every rank runs an independent replica on its own
+field (the path has no cross-field exchange): weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sites/s 5-loop Fmunu+B^2 fwd+bwd @32^3x64: FP32 vs FP64 GPU, ≤1e-6 rel, %HBM"
+# algorithmic bytes per site of one fwd+bwd (3 spatial links read for the
+# forward, read again for the backward, a 4-direction gradient written in U's
+# dtype): FP64 1440, FP32-18 720, FP32-r12 576
+ALG_BYTES = {"c128": 1440, "c64": 720, "r12": 576}
+# matrix products per site of one fwd+bwd as this implementation structures it:
+# lines 6, forward 3 planes x 28 leaves x 3, line cotangents 3 dirs x (96+64+64),
+# link cotangents 3 x 7; 198 flop per 3x3 complex product (27 cmul + 18 cadd)
+PRODUCTS_PER_SITE = {"lines": 6, "fwd": 252, "linecot": 672, "linkcot": 21}
+FLOP_PER_PRODUCT = 198
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--prec", choices=["r12", "c64"], default="r12")
+    p.add_argument("--dims", default="64,32,32,32", help="NT,NX,NY,NZ")
+    p.add_argument("--eps", type=float, default=0.3)
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--fp64-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.15)
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(host_c128, dims, target_s):
+    """The oracle's OpenMP magnetic() on a bounded slab of time slices."""
+    import oracle
+
+    nt = dims[0]
+    V3 = dims[1] * dims[2] * dims[3]
+    t0 = time.perf_counter()
+    oracle.magnetic_slab(host_c128, 1, 1)
+    one = max(time.perf_counter() - t0, 1e-3)
+    nsl = int(max(1, min(nt, target_s / one)))
+    t0 = time.perf_counter()
+    oracle.magnetic_slab(host_c128, 1, nsl)
+    dt = time.perf_counter() - t0
+    return {"value": nsl * V3 / dt, "unit": "sites/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"oracle magnetic() forward (B^2 only; the reference has no backward), OpenMP, time slices "
+                      f"1..{nsl} of the {dims[1]}^3x{dims[0]} field ({nsl * V3} sites, {dt:.2f} s)"}
+
+
+def run_reference(args, dims, ws, rank):
+    """--impl reference: the reference's algorithm (oracle port of wloops.F90
+    magnetic(), forward only) on the host cores; rank 0 only."""
+    if rank != 0:
+        return
+    import numpy as np
+
+    import oracle
+    from flue_gb300 import generate
+
+    oracle.build()
+    # host field of the same configuration (generated slab-wise is not
+    # needed: the whole field is built once, then each step times a slab)
+    nt, nx, ny, nz = dims
+    U = generate_host_field(dims, args.eps, args.seed)
+    V3 = nx * ny * nz
+    t0 = time.perf_counter()
+    oracle.magnetic_slab(U, 1, 1)
+    one = max(time.perf_counter() - t0, 1e-3)
+    per_step_s = max(1.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
+    nsl = int(max(1, min(nt, per_step_s / one)))
+    for _ in range(args.warmup):
+        oracle.magnetic_slab(U, 1, nsl)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.magnetic_slab(U, 1, nsl)
+    dt = (time.perf_counter() - t0) / args.steps
+    val = nsl * V3 / dt
+    line = {"metric": METRIC, "value": val, "unit": "sites/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"magnetic() B^2 forward, {nx}^3x{nt}", "global_batch": 1, "seq_len": None,
+                       "parallelism": "host OpenMP", "eps": args.eps, "seed": args.seed},
+            "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": "sites/s", "cores": oracle.num_threads(), "kind": "port",
+                             "sample": f"per step: time slices 1..{nsl} of the field ({nsl * V3} sites), forward only "
+                                       "(the reference has no backward); Fortran reference not buildable here, "
+                                       "C restatement of src/wloops.F90 timed instead"},
+            "e2e": {"value": val, "unit": "sites/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def generate_host_field(dims, eps, seed):
+    """FP64 host copy of the benchmark field (exponentials on the GPU when one
+    is present, so that the 32^3x64 field builds in seconds)."""
+    import torch
+
+    from flue_gb300 import generate
+
+    if torch.cuda.is_available():
+        return generate.random_field(dims, eps, seed, device="cuda").to_numpy()
+    return generate.random_field(dims, eps, seed)
+
+
+def main():
+    args = parse()
+    dims = tuple(int(v) for v in args.dims.split(","))
+    nt, nx, ny, nz = dims
+    V = nt * nx * ny * nz
+    if args.impl == "reference":
+        ws = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, dims, ws, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    from flue_gb300 import _lib, generate
+    from flue_gb300.field import GaugeField, _ptr, workspace
+
+    wsz, rank, local = dist_setup(args)
+    L = _lib.load()
+    dev = torch.device("cuda", local if wsz > 1 else 0)
+    stream = torch.cuda.current_stream()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+
+    # --- fields (per rank: its own replica, seed offset by rank) ---
+    f64 = generate.random_field(dims, args.eps, args.seed + rank, device=dev)
+    f32 = GaugeField.from_array(f64, prec=args.prec)
+
+    def prep(f):
+        w = workspace(_lib.OP_MAGNETIC_FORCE, f).clone()
+        out = torch.empty(1, dtype=torch.float64, device=dev)
+        force = torch.empty((3, 3, 4, nz, ny, nx, nt), dtype=f.compute_dtype, device=dev)
+        return f.descriptor(), w, out, force
+
+    d32, w32, b32, g32 = prep(f32)
+
+    def step32():
+        rc = L.flue_magnetic_force(ctypes.byref(d32), _ptr(b32), _ptr(g32), _lib.FORCE_LIE, _ptr(w32), w32.numel(), sh)
+        if rc:
+            raise RuntimeError(L.flue_last_error_detail().decode())
+
+    for _ in range(args.warmup):
+        step32()
+    torch.cuda.synchronize()
+    barrier(wsz)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            step32()
+        e1.record()
+        torch.cuda.synchronize()
+    barrier(wsz)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(wsz, ms)
+    value = wsz * V / (ms * 1e-3)
+
+    # --- per-stage timing of one step (CUDA events between the launches) ---
+    L.flue_stage_timing(1)
+    stage_ms = {k: 0.0 for k in ("lines", "fwd", "linecot", "linkcot")}
+    nrep = min(10, args.steps)
+    for _ in range(nrep):
+        step32()
+        buf = (ctypes.c_double * 8)()
+        n = ctypes.c_int()
+        L.flue_stage_times(buf, 8, ctypes.byref(n))
+        for k, name in enumerate(("lines", "fwd", "linecot", "linkcot")[: n.value]):
+            stage_ms[name] += buf[k] / nrep
+    L.flue_stage_timing(0)
+    torch.cuda.synchronize()
+
+    # --- FP64 (complex128) GPU kernels: the denominator of the FP32 speed-up ---
+    d64, w64, b64, g64 = prep(f64)
+
+    def step64():
+        rc = L.flue_magnetic_force(ctypes.byref(d64), _ptr(b64), _ptr(g64), _lib.FORCE_LIE, _ptr(w64), w64.numel(), sh)
+        if rc:
+            raise RuntimeError(L.flue_last_error_detail().decode())
+
+    step64()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.fp64_steps):
+        step64()
+    e1.record()
+    torch.cuda.synchronize()
+    ms64 = max_over_ranks(wsz, e0.elapsed_time(e1) / args.fp64_steps)
+    value64 = wsz * V / (ms64 * 1e-3)
+
+    # --- FP32 error against the FP64 result on the same field ---
+    step32()
+    torch.cuda.synchronize()
+    B32, B64 = b32.item(), b64.item()
+    rel_b = abs(B32 - B64) / abs(B64)
+    gdiff = torch.linalg.vector_norm((g32.to(torch.complex128) - g64).flatten()).item()
+    gnorm = torch.linalg.vector_norm(g64.flatten()).item()
+    rel_g = gdiff / gnorm
+    gmax = ((g32.to(torch.complex128) - g64).abs().max() / g64.abs().max()).item()
+    del w64, g64
+    torch.cuda.empty_cache()
+
+    # --- end to end through the host-buffer C ABI (pinned host buffers) ---
+    host_in = f32.to_tensor(torch.complex64).permute(6, 5, 4, 3, 2, 1, 0).contiguous().cpu().pin_memory()
+    host_grad = torch.empty_like(host_in).pin_memory()
+    hb = ctypes.c_double()
+    prec_code = {"r12": _lib.R12, "c64": _lib.C64}[args.prec]
+
+    def e2e_step():
+        rc = L.flue_magnetic_force_c(ctypes.c_void_p(host_in.data_ptr()), _lib.C64, nt, nx, ny, nz, prec_code,
+                                     _lib.FORCE_LIE, ctypes.byref(hb), ctypes.c_void_p(host_grad.data_ptr()))
+        if rc:
+            raise RuntimeError(L.flue_last_error_detail().decode())
+
+    e2e_step()
+    barrier(wsz)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_s = max_over_ranks(wsz, e2e_s)
+    L.flue_release_host_cache()
+    e2e_val = wsz * V / e2e_s
+    h2d = host_in.numel() * host_in.element_size()
+
+    # --- CPU baseline (rank 0, N = 1 only) ---
+    cpu = None
+    cpu_b2 = None
+    if rank == 0 and wsz == 1 and not args.no_cpu:
+        import oracle
+
+        oracle.build()
+        host64 = f64.to_numpy()
+        cpu = cpu_baseline(host64, dims, args.cpu_seconds)
+
+    # --- roofline ---
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    alg_bytes = ALG_BYTES[args.prec] * V
+    achieved_gbs = alg_bytes / (ms * 1e-3) / 1e9 / wsz * wsz  # per GPU
+    achieved_gbs = ALG_BYTES[args.prec] * V / (ms * 1e-3) / 1e9
+    clk = clk.summary()
+    sm_mhz = clk["sm_mhz"] or 1900.0
+    # FP32 CUDA-core peak at the sampled clock: 152 SMs x 128 lanes x 2 flop
+    fp32_peak_tflops = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    lc_ms = stage_ms["linecot"] or ms
+    lc_flops = PRODUCTS_PER_SITE["linecot"] * FLOP_PER_PRODUCT * V
+    lc_tflops = lc_flops / (lc_ms * 1e-3) / 1e12
+    step_flops = sum(PRODUCTS_PER_SITE.values()) * FLOP_PER_PRODUCT * V
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "sites/s",
+        "n_gpus": wsz,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"5-loop F_munu + B^2 forward + backward (su(3) gradient), {nx}^3x{nt}",
+                   "lattice": [nt, nx, ny, nz], "sites": V, "field_format": args.prec, "eps": args.eps,
+                   "seed": args.seed, "global_batch": wsz, "parallelism": f"replicas x{wsz}",
+                   "l2": "inputs and intermediates larger than L2 (field 0.4-0.6 GB, 2.5 GB scratch per step)"},
+        "fp64": {"value": value64, "unit": "sites/s", "ms_per_step": ms64, "steps": args.fp64_steps},
+        "fp32_over_fp64": value / value64,
+        "fp32_error_vs_fp64": {"b2_rel": rel_b, "grad_rel_l2": rel_g, "grad_rel_max": gmax, "b2_fp64": B64},
+        "stages_ms": stage_ms,
+        "gpu_launches": args.steps * 5,
+        "e2e": {"value": e2e_val, "unit": "sites/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d + 8,
+                "s_per_step": e2e_s, "api": "flue_magnetic_force_c (host complex64 in, host gradient out)"},
+        "roofline": {"bound": "hbm", "kernel": "whole fwd+bwd step (metric's %HBM)", "achieved": achieved_gbs,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak, "traffic": None,
+                     "peak_source": peak_src, "alg_bytes_per_site": ALG_BYTES[args.prec]},
+        "compute_roofline": {"bound": "fp32_cuda_core", "kernel": "k_linecot (line cotangents)",
+                             "achieved": lc_tflops, "peak": fp32_peak_tflops, "unit": "TFLOP/s",
+                             "frac": lc_tflops / fp32_peak_tflops,
+                             "step_tflops": step_flops / (ms * 1e-3) / 1e12,
+                             "peak_basis": "152 SM x 128 FP32 lanes x 2 flop x median sampled SM clock"},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if wsz > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,685 @@
+// capi.cu -- the extern "C" boundary declared in include/flue_gb300.h.
+// Validates every argument on the host, maps CUDA errors to status codes
+// and never exits or traps.  The host-buffer tier keeps one set of device
+// buffers and one stream per device, guarded by a mutex.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "../../include/flue_gb300.h"
+#include "flue_internal.h"
+
+using namespace flue;
+
+namespace {
+
+thread_local char g_detail[256] = "";
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return FLUE_OK;
+    snprintf(g_detail, sizeof(g_detail), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
+    return FLUE_ERR_CUDA;
+}
+int fail(int code, const char* msg) {
+    snprintf(g_detail, sizeof(g_detail), "%s", msg);
+    return code;
+}
+
+bool dims_ok(int nt, int nx, int ny, int nz) {
+    if (nt < 1 || nx < 1 || ny < 1 || nz < 1) return false;
+    const int64_t V = (int64_t)nt * nx * ny * nz;
+    return V < ((int64_t)1 << 31);  // nP of one plane is a default integer, as in the reference
+}
+bool prec_ok(int p) { return p == FLUE_C128 || p == FLUE_C64 || p == FLUE_R12; }
+
+int check_field(const flue_field* U, FieldRef* out) {
+    if (!U) return fail(FLUE_ERR_ARG, "field descriptor is NULL");
+    if (!U->links) return fail(FLUE_ERR_ARG, "field links pointer is NULL");
+    if (!prec_ok(U->prec)) return fail(FLUE_ERR_DTYPE, "unknown field precision");
+    if (!dims_ok(U->nt, U->nx, U->ny, U->nz)) return fail(FLUE_ERR_SHAPE, "bad lattice extents");
+    const uintptr_t align = U->prec == FLUE_C64 ? 8 : 16;
+    if (((uintptr_t)U->links) % align) return fail(FLUE_ERR_LAYOUT, "field pointer misaligned");
+    out->links = U->links;
+    out->g = make_geom(U->nt, U->nx, U->ny, U->nz);
+    out->prec = U->prec;
+    return FLUE_OK;
+}
+
+inline size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+PlaneSet b2_planes() {
+    // magnetic: Loop5(3,2), Loop5(2,4), Loop5(4,3)  (src/wloops.F90:502-506)
+    PlaneSet ps;
+    ps.np = 3;
+    ps.mu[0] = 2, ps.nu[0] = 1;
+    ps.mu[1] = 1, ps.nu[1] = 3;
+    ps.mu[2] = 3, ps.nu[2] = 2;
+    return ps;
+}
+PlaneSet all_planes() {
+    PlaneSet ps;
+    ps.np = 0;
+    for (int m = 0; m < 4; ++m)
+        for (int n = m + 1; n < 4; ++n) {
+            ps.mu[ps.np] = m;
+            ps.nu[ps.np] = n;
+            ps.np++;
+        }
+    return ps;
+}
+
+size_t ws_bytes_for(int op, const Geom& g, int prec) {
+    switch (op) {
+        case FLUE_OP_PLAQUETTE:
+            return a256((size_t)plaquette_blocks(g) * 8);
+        case FLUE_OP_POLYAKOV:
+            return a256((size_t)polyakov_blocks(g) * 16);
+        case FLUE_OP_WMUNU:
+            return a256((size_t)wloop_blocks(g) * 8);
+        case FLUE_OP_FMUNU: {
+            PlaneSet ps;
+            ps.np = 1;
+            ps.mu[0] = 0;
+            ps.nu[0] = 1;
+            return energy_ws_bytes(g, prec, ps, false);
+        }
+        case FLUE_OP_MAGNETIC:
+            return energy_ws_bytes(g, prec, b2_planes(), false);
+        case FLUE_OP_MAGNETIC_FORCE:
+            return energy_ws_bytes(g, prec, b2_planes(), true);
+        case FLUE_OP_ENERGY_FORCE:
+            return energy_ws_bytes(g, prec, all_planes(), true);
+        case FLUE_OP_PLAQUETTE_FORCE:
+            return a256((size_t)plaqforce_blocks(g) * 4 * 8);
+        case FLUE_OP_MEANLINK:
+            return a256((size_t)meanlink_blocks(g) * 4 * 8);
+        case FLUE_OP_WFLOW:
+            return wflow_ws_bytes(g);
+        default:
+            return 0;
+    }
+}
+
+int check_ws(int op, const FieldRef& F, size_t ws_bytes, const void* ws) {
+    const size_t need = ws_bytes_for(op, F.g, F.prec);
+    if (need && (!ws || ws_bytes < need)) {
+        snprintf(g_detail, sizeof(g_detail), "workspace too small: need %zu bytes, got %zu", need, ws_bytes);
+        return FLUE_ERR_WORKSPACE;
+    }
+    if (ws && ((uintptr_t)ws) % 256) return fail(FLUE_ERR_LAYOUT, "workspace must be 256-byte aligned");
+    return FLUE_OK;
+}
+
+int energy_common(const flue_field* U, const PlaneSet& ps, int op, double* d_E, void* d_force, int form, void* ws,
+                  size_t ws_bytes, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (form != FLUE_FORCE_LIE && form != FLUE_FORCE_EUCLID) return fail(FLUE_ERR_ARG, "bad force form");
+    if (!d_E && !d_force) return fail(FLUE_ERR_ARG, "nothing to compute");
+    const size_t need = energy_ws_bytes(F.g, F.prec, ps, d_force != nullptr);
+    if (!ws || ws_bytes < need) {
+        snprintf(g_detail, sizeof(g_detail), "workspace too small: need %zu bytes, got %zu", need, ws_bytes);
+        return FLUE_ERR_WORKSPACE;
+    }
+    (void)op;
+    return cuda_status(launch_energy(F, ps, d_E, d_force, form, ws, ws_bytes, (cudaStream_t)stream));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* flue_strerror(int s) {
+    switch (s) {
+        case FLUE_OK:
+            return "ok";
+        case FLUE_ERR_ARG:
+            return "invalid argument";
+        case FLUE_ERR_SHAPE:
+            return "invalid lattice shape";
+        case FLUE_ERR_DTYPE:
+            return "invalid precision / dtype";
+        case FLUE_ERR_LAYOUT:
+            return "unsupported layout / alignment";
+        case FLUE_ERR_CUDA:
+            return "CUDA runtime error";
+        case FLUE_ERR_TIMEOUT:
+            return "bounded device wait timed out";
+        case FLUE_ERR_WORKSPACE:
+            return "workspace too small";
+        case FLUE_ERR_NOMEM:
+            return "device allocation failed";
+        default:
+            return "unknown status";
+    }
+}
+
+// Detail of the most recent failure on this thread (not part of the
+// reference interface; diagnostic only).
+const char* flue_last_error_detail(void) { return g_detail; }
+
+int flue_abi_version(void) { return 1; }
+
+int flue_stage_timing(int enable) { return cuda_status(stage_timing_enable(enable)); }
+
+int flue_stage_times(double* ms, int max_stages, int* n_stages) {
+    if (!ms || !n_stages || max_stages < 0) return fail(FLUE_ERR_ARG, "NULL pointer");
+    return cuda_status(stage_times(ms, max_stages, n_stages));
+}
+
+int64_t flue_field_bytes(int nt, int nx, int ny, int nz, int prec) {
+    if (!dims_ok(nt, nx, ny, nz) || !prec_ok(prec)) return -1;
+    const int64_t V = (int64_t)nt * nx * ny * nz;
+    if (prec == FLUE_C128) return V * 36 * 16;
+    if (prec == FLUE_C64) return V * 36 * 8;
+    return V * 12 * 16;
+}
+
+size_t flue_workspace_bytes(int op, int nt, int nx, int ny, int nz, int prec) {
+    if (!dims_ok(nt, nx, ny, nz) || !prec_ok(prec)) return 0;
+    return ws_bytes_for(op, make_geom(nt, nx, ny, nz), prec);
+}
+
+int flue_pack_field(const void* src, int src_dtype, const int64_t strides[7], int nt, int nx, int ny, int nz, void* dst,
+                    int dst_prec, int reunitarise, void* stream) {
+    if (!src || !dst || !strides) return fail(FLUE_ERR_ARG, "NULL pointer");
+    if (src_dtype != FLUE_C128 && src_dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "source must be c128 or c64");
+    if (!prec_ok(dst_prec)) return fail(FLUE_ERR_DTYPE, "bad destination precision");
+    if (!dims_ok(nt, nx, ny, nz)) return fail(FLUE_ERR_SHAPE, "bad lattice extents");
+    for (int k = 0; k < 7; ++k)
+        if (strides[k] < 0) return fail(FLUE_ERR_LAYOUT, "negative strides are not supported");
+    const Geom g = make_geom(nt, nx, ny, nz);
+    return cuda_status(launch_pack(src, src_dtype, strides, g, dst, dst_prec, reunitarise, (cudaStream_t)stream));
+}
+
+int flue_unpack_field(const flue_field* U, void* dst, int dst_dtype, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!dst) return fail(FLUE_ERR_ARG, "NULL destination");
+    if (dst_dtype != FLUE_C128 && dst_dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "destination must be c128 or c64");
+    return cuda_status(launch_unpack(F, dst, dst_dtype, (cudaStream_t)stream));
+}
+
+int flue_reunitarise_field(const flue_field* U, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    return cuda_status(launch_fix_field((void*)F.links, F.g, F.prec, (cudaStream_t)stream));
+}
+
+int flue_multiplymatmat_batch(const void* left, const void* right, void* out, int64_t n, int dtype, int dagger,
+                              void* stream) {
+    if (!left || !right || !out) return fail(FLUE_ERR_ARG, "NULL pointer");
+    if (n < 0) return fail(FLUE_ERR_SHAPE, "negative count");
+    if (dtype != FLUE_C128 && dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "dtype must be c128 or c64");
+    if (n == 0) return FLUE_OK;
+    return cuda_status(launch_matmul_batch(left, right, out, n, dtype, dagger, (cudaStream_t)stream));
+}
+
+int flue_plaquette(const flue_field* U, int muStart, int muEnd, int nuEnd, double* d_sum, void* ws, size_t ws_bytes,
+                   void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_sum) return fail(FLUE_ERR_ARG, "NULL output");
+    if (muStart < 1 || muEnd > 4 || nuEnd > 4 || muStart > muEnd + 1 || nuEnd < 1)
+        return fail(FLUE_ERR_ARG, "plane range out of 1..4");
+    if ((rc = check_ws(FLUE_OP_PLAQUETTE, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_plaquette(F, muStart - 1, muEnd - 1, nuEnd - 1, (double*)ws, d_sum, (cudaStream_t)stream));
+}
+
+int flue_polyakov(const flue_field* U, double* d_sum2, void* ws, size_t ws_bytes, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_sum2) return fail(FLUE_ERR_ARG, "NULL output");
+    if ((rc = check_ws(FLUE_OP_POLYAKOV, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_polyakov(F, (double*)ws, d_sum2, (cudaStream_t)stream));
+}
+
+int flue_wmunu(const flue_field* U, int tau, int mu, int nu, int nMu, int nNu, double* d_val, void* ws, size_t ws_bytes,
+               void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_val) return fail(FLUE_ERR_ARG, "NULL output");
+    if (mu < 1 || mu > 4 || nu < 1 || nu > 4) return fail(FLUE_ERR_ARG, "direction out of 1..4");
+    if (nMu < 1 || nNu < 1) return fail(FLUE_ERR_ARG, "loop extents must be >= 1");
+    if (tau < 0 || tau > U->nt) return fail(FLUE_ERR_ARG, "tau out of 0..NT");
+    if ((rc = check_ws(FLUE_OP_WMUNU, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_wloop(F, tau - 1, mu - 1, nu - 1, nMu, nNu, (double*)ws, d_val, (cudaStream_t)stream));
+}
+
+int flue_genericpath(const flue_field* U, const int* coordBase, const int* path, int npath, void* d_out, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_out || (!path && npath > 0)) return fail(FLUE_ERR_ARG, "NULL pointer");
+    if (npath < 0 || npath > 256) return fail(FLUE_ERR_ARG, "path length must be 0..256");
+    for (int k = 0; k < npath; ++k)
+        if (path[k] == 0 || path[k] < -4 || path[k] > 4) return fail(FLUE_ERR_ARG, "path entry out of +-1..+-4");
+    if (coordBase) {
+        const int n[4] = {U->nt, U->nx, U->ny, U->nz};
+        for (int k = 0; k < 4; ++k)
+            if (coordBase[k] < 1 || coordBase[k] > n[k]) return fail(FLUE_ERR_ARG, "coordBase out of range");
+    }
+    return cuda_status(launch_genericpath(F, path, npath, coordBase, d_out, (cudaStream_t)stream));
+}
+
+int flue_fmunu(const flue_field* U, int kind, int mu, int nu, void* d_out, void* ws, size_t ws_bytes, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_out) return fail(FLUE_ERR_ARG, "NULL output");
+    if (kind != FLUE_FMUNU_CLOVER && kind != FLUE_FMUNU_LOOP5) return fail(FLUE_ERR_ARG, "bad F_munu kind");
+    if (mu < 1 || mu > 4 || nu < 1 || nu > 4 || mu == nu) return fail(FLUE_ERR_ARG, "bad plane");
+    if ((rc = check_ws(FLUE_OP_FMUNU, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_fmunu(F, kind, mu - 1, nu - 1, d_out, ws, ws_bytes, (cudaStream_t)stream));
+}
+
+int flue_magnetic(const flue_field* U, double* d_B, void* ws, size_t ws_bytes, void* stream) {
+    if (!d_B) return fail(FLUE_ERR_ARG, "NULL output");
+    return energy_common(U, b2_planes(), FLUE_OP_MAGNETIC, d_B, nullptr, FLUE_FORCE_LIE, ws, ws_bytes, stream);
+}
+
+int flue_magnetic_force(const flue_field* U, double* d_B, void* d_force, int force_form, void* ws, size_t ws_bytes,
+                        void* stream) {
+    return energy_common(U, b2_planes(), FLUE_OP_MAGNETIC_FORCE, d_B, d_force, force_form, ws, ws_bytes, stream);
+}
+
+int flue_loop5_energy_force(const flue_field* U, const int* planes, int nplanes, double* d_E, void* d_force,
+                            int force_form, void* ws, size_t ws_bytes, void* stream) {
+    if (!planes || nplanes < 1 || nplanes > 6) return fail(FLUE_ERR_ARG, "nplanes must be 1..6");
+    PlaneSet ps;
+    ps.np = nplanes;
+    int seen = 0;
+    for (int p = 0; p < nplanes; ++p) {
+        const int m = planes[2 * p], n = planes[2 * p + 1];
+        if (m < 1 || m > 4 || n < 1 || n > 4 || m == n) return fail(FLUE_ERR_ARG, "bad plane");
+        const int lo = m < n ? m : n, hi = m < n ? n : m;
+        const int bit = 1 << (lo * 4 + hi);
+        if (seen & bit) return fail(FLUE_ERR_ARG, "plane listed twice");
+        seen |= bit;
+        ps.mu[p] = m - 1;
+        ps.nu[p] = n - 1;
+    }
+    return energy_common(U, ps, FLUE_OP_ENERGY_FORCE, d_E, d_force, force_form, ws, ws_bytes, stream);
+}
+
+int flue_plaquette_force(const flue_field* U, double* d_S, void* d_force, int force_form, void* ws, size_t ws_bytes,
+                         void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_S && !d_force) return fail(FLUE_ERR_ARG, "nothing to compute");
+    if (force_form != FLUE_FORCE_LIE && force_form != FLUE_FORCE_EUCLID) return fail(FLUE_ERR_ARG, "bad force form");
+    if ((rc = check_ws(FLUE_OP_PLAQUETTE_FORCE, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_plaquette_force(F, (double*)ws, d_S, d_force, force_form, (cudaStream_t)stream));
+}
+
+int flue_meanlink(const flue_field* U, const void* G, int g_dtype, double* d_sum4, void* ws, size_t ws_bytes,
+                  void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!G || !d_sum4) return fail(FLUE_ERR_ARG, "NULL pointer");
+    if (g_dtype != FLUE_C128 && g_dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "G must be c128 or c64");
+    if ((rc = check_ws(FLUE_OP_MEANLINK, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_meanlink(F, G, g_dtype, (double*)ws, d_sum4, (cudaStream_t)stream));
+}
+
+int flue_wflow_step(const flue_field* U, double eps, void* ws, size_t ws_bytes, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (F.prec == FLUE_R12) return fail(FLUE_ERR_DTYPE, "Wilson flow needs a C128 or C64 field");
+    if (!(eps > 0.0) || !isfinite(eps)) return fail(FLUE_ERR_ARG, "eps must be positive");
+    if ((rc = check_ws(FLUE_OP_WFLOW, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_wflow_step((void*)F.links, F.g, F.prec, eps, ws, (cudaStream_t)stream));
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Host-buffer tier
+// ===========================================================================
+namespace {
+
+struct DevCache {
+    std::mutex mtx;
+    bool init = false;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    void* field = nullptr;
+    size_t field_bytes = 0;
+    void* field2 = nullptr;
+    size_t field2_bytes = 0;
+    void* ws = nullptr;
+    size_t ws_bytes = 0;
+    void* out = nullptr;
+    size_t out_bytes = 0;
+    double* scal = nullptr;
+};
+
+std::mutex g_cache_mtx;
+std::vector<DevCache*> g_caches;
+
+int grow(void** p, size_t* have, size_t need) {
+    if (*have >= need && *p) return FLUE_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    cudaError_t e = cudaMalloc(p, need < 256 ? 256 : need);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(FLUE_ERR_NOMEM, "device allocation failed in the host-buffer tier");
+    }
+    *have = need;
+    return FLUE_OK;
+}
+
+DevCache* cache_for_current(int* rc) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *rc = cuda_status(e);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_cache_mtx);
+    if ((int)g_caches.size() <= dev) g_caches.resize(dev + 1, nullptr);
+    if (!g_caches[dev]) g_caches[dev] = new DevCache();
+    DevCache* c = g_caches[dev];
+    if (!c->init) {
+        if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreate(&c->e0)) != cudaSuccess || (e = cudaEventCreate(&c->e1)) != cudaSuccess ||
+            (e = cudaMalloc((void**)&c->scal, 64 * sizeof(double))) != cudaSuccess) {
+            *rc = cuda_status(e);
+            return nullptr;
+        }
+        c->init = true;
+    }
+    *rc = FLUE_OK;
+    return c;
+}
+
+// Upload a host complex128 field (Fortran order) into the cache's field
+// buffer; the reference layout IS the FLUE_C128 device layout.
+int upload_c128(DevCache* c, const double* data, int nt, int nx, int ny, int nz, flue_field* U) {
+    if (!data) return fail(FLUE_ERR_ARG, "NULL data");
+    if (!dims_ok(nt, nx, ny, nz)) return fail(FLUE_ERR_SHAPE, "bad lattice extents");
+    const size_t bytes = (size_t)flue_field_bytes(nt, nx, ny, nz, FLUE_C128);
+    int rc = grow(&c->field, &c->field_bytes, bytes);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(c->field, data, bytes, cudaMemcpyHostToDevice, c->st);
+    if (e != cudaSuccess) return cuda_status(e);
+    U->links = c->field;
+    U->nt = nt;
+    U->nx = nx;
+    U->ny = ny;
+    U->nz = nz;
+    U->prec = FLUE_C128;
+    return FLUE_OK;
+}
+
+int ensure_ws(DevCache* c, int op, const flue_field& U) {
+    const size_t need = flue_workspace_bytes(op, U.nt, U.nx, U.ny, U.nz, U.prec);
+    return grow(&c->ws, &c->ws_bytes, need);
+}
+
+int fetch(DevCache* c, void* host, const void* dev, size_t bytes) {
+    cudaError_t e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->st);
+    if (e != cudaSuccess) return cuda_status(e);
+    return cuda_status(cudaStreamSynchronize(c->st));
+}
+
+double elapsed_s(DevCache* c) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->e0, c->e1);
+    return (double)ms * 1e-3;
+}
+
+}  // namespace
+
+#define HOST_PROLOGUE()                        \
+    int rc = FLUE_OK;                          \
+    DevCache* c = cache_for_current(&rc);      \
+    if (!c) return rc;                         \
+    std::lock_guard<std::mutex> lk(c->mtx)
+
+extern "C" {
+
+static int plaq_host(const double* data, int NT, int NX, int NY, int NZ, int muStart, int muEnd, int nuEnd,
+                     double* sumTrP, int* nP, double* time) {
+    if (!sumTrP || !nP || !time) return fail(FLUE_ERR_ARG, "NULL output");
+    HOST_PROLOGUE();
+    flue_field U;
+    if ((rc = upload_c128(c, data, NT, NX, NY, NZ, &U))) return rc;
+    if ((rc = ensure_ws(c, FLUE_OP_PLAQUETTE, U))) return rc;
+    cudaEventRecord(c->e0, c->st);
+    if ((rc = flue_plaquette(&U, muStart, muEnd, nuEnd, c->scal, c->ws, c->ws_bytes, c->st))) return rc;
+    cudaEventRecord(c->e1, c->st);
+    double s = 0.0;
+    if ((rc = fetch(c, &s, c->scal, sizeof(double)))) return rc;
+    int np = 0;
+    for (int mu = muStart; mu <= muEnd; ++mu)
+        for (int nu = mu + 1; nu <= nuEnd; ++nu) np++;
+    *sumTrP = s;
+    *nP = (int)((int64_t)np * NT * NX * NY * NZ);
+    *time = elapsed_s(c);
+    return FLUE_OK;
+}
+
+int flue_plaquette_c(const double* data, int NT, int NX, int NY, int NZ, int muStart, int muEnd, int nuEnd,
+                     double* sumTrP, int* nP, double* time) {
+    return plaq_host(data, NT, NX, NY, NZ, muStart, muEnd, nuEnd, sumTrP, nP, time);
+}
+
+int flue_genplaquette_c(const double* data, int NT, int NX, int NY, int NZ, int muStart, int muEnd, int nuEnd,
+                        double* sumTrP, int* nP, double* time) {
+    return plaq_host(data, NT, NX, NY, NZ, muStart, muEnd, nuEnd, sumTrP, nP, time);
+}
+
+int flue_polyakov_c(const double* data, int NT, int NX, int NY, int NZ, double* sumTrP, int* nP, double* time) {
+    if (!sumTrP || !nP || !time) return fail(FLUE_ERR_ARG, "NULL output");
+    HOST_PROLOGUE();
+    flue_field U;
+    if ((rc = upload_c128(c, data, NT, NX, NY, NZ, &U))) return rc;
+    if ((rc = ensure_ws(c, FLUE_OP_POLYAKOV, U))) return rc;
+    cudaEventRecord(c->e0, c->st);
+    if ((rc = flue_polyakov(&U, c->scal, c->ws, c->ws_bytes, c->st))) return rc;
+    cudaEventRecord(c->e1, c->st);
+    double s[2];
+    if ((rc = fetch(c, s, c->scal, 2 * sizeof(double)))) return rc;
+    *sumTrP = s[0];
+    *nP = NX * NY * NZ;
+    *time = elapsed_s(c);
+    return FLUE_OK;
+}
+
+int flue_genericpath_c(const double* data, int NT, int NX, int NY, int NZ, const int* coordBase, const int* path,
+                       int npath, double* U_xd) {
+    if (!U_xd || !coordBase) return fail(FLUE_ERR_ARG, "NULL pointer");
+    HOST_PROLOGUE();
+    flue_field U;
+    if ((rc = upload_c128(c, data, NT, NX, NY, NZ, &U))) return rc;
+    if ((rc = grow(&c->out, &c->out_bytes, 9 * 16))) return rc;
+    if ((rc = flue_genericpath(&U, coordBase, path, npath, c->out, c->st))) return rc;
+    return fetch(c, U_xd, c->out, 9 * 16);
+}
+
+static int wloop_host(const double* data, int NT, int NX, int NY, int NZ, int tau, int mu, int nu, int nMu, int nNu,
+                      double* loopVal) {
+    if (!loopVal) return fail(FLUE_ERR_ARG, "NULL output");
+    HOST_PROLOGUE();
+    flue_field U;
+    if ((rc = upload_c128(c, data, NT, NX, NY, NZ, &U))) return rc;
+    if ((rc = ensure_ws(c, FLUE_OP_WMUNU, U))) return rc;
+    if ((rc = flue_wmunu(&U, tau, mu, nu, nMu, nNu, c->scal, c->ws, c->ws_bytes, c->st))) return rc;
+    return fetch(c, loopVal, c->scal, sizeof(double));
+}
+
+int flue_wmunu_c(const double* data, int NT, int NX, int NY, int NZ, int mu, int nu, int nMu, int nNu, double* loopVal) {
+    return wloop_host(data, NT, NX, NY, NZ, 0, mu, nu, nMu, nNu, loopVal);
+}
+
+int flue_wmunutau_c(const double* data, int NT, int NX, int NY, int NZ, int tau, int mu, int nu, int nMu, int nNu,
+                    double* loopVal) {
+    if (tau < 1) return fail(FLUE_ERR_ARG, "tau out of 1..NT");
+    return wloop_host(data, NT, NX, NY, NZ, tau, mu, nu, nMu, nNu, loopVal);
+}
+
+static int fmunu_host(const double* data, int NT, int NX, int NY, int NZ, int kind, int mu, int nu, double* U_xd) {
+    if (!U_xd) return fail(FLUE_ERR_ARG, "NULL output");
+    HOST_PROLOGUE();
+    flue_field U;
+    if ((rc = upload_c128(c, data, NT, NX, NY, NZ, &U))) return rc;
+    if ((rc = ensure_ws(c, FLUE_OP_FMUNU, U))) return rc;
+    const size_t ob = (size_t)NT * NX * NY * NZ * 9 * 16;
+    if ((rc = grow(&c->out, &c->out_bytes, ob))) return rc;
+    if ((rc = flue_fmunu(&U, kind, mu, nu, c->out, c->ws, c->ws_bytes, c->st))) return rc;
+    return fetch(c, U_xd, c->out, ob);
+}
+
+int flue_cloverloopmunucoord_c(const double* data, int NT, int NX, int NY, int NZ, int mu, int nu, double* U_xd) {
+    return fmunu_host(data, NT, NX, NY, NZ, FLUE_FMUNU_CLOVER, mu, nu, U_xd);
+}
+
+int flue_loop5munucoord_c(const double* data, int NT, int NX, int NY, int NZ, int mu, int nu, double* U_xd) {
+    return fmunu_host(data, NT, NX, NY, NZ, FLUE_FMUNU_LOOP5, mu, nu, U_xd);
+}
+
+int flue_magnetic_c(const double* data, int NT, int NX, int NY, int NZ, double* B) {
+    if (!B) return fail(FLUE_ERR_ARG, "NULL output");
+    HOST_PROLOGUE();
+    flue_field U;
+    if ((rc = upload_c128(c, data, NT, NX, NY, NZ, &U))) return rc;
+    if ((rc = ensure_ws(c, FLUE_OP_MAGNETIC, U))) return rc;
+    if ((rc = flue_magnetic(&U, c->scal, c->ws, c->ws_bytes, c->st))) return rc;
+    return fetch(c, B, c->scal, sizeof(double));
+}
+
+int flue_multiplymatmat_c(double* MM, const double* left, const double* right) {
+    if (!MM || !left || !right) return fail(FLUE_ERR_ARG, "NULL pointer");
+    HOST_PROLOGUE();
+    if ((rc = grow(&c->out, &c->out_bytes, 3 * 9 * 16))) return rc;
+    char* o = (char*)c->out;
+    cudaError_t e = cudaMemcpyAsync(o, left, 9 * 16, cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(o + 9 * 16, right, 9 * 16, cudaMemcpyHostToDevice, c->st);
+    if (e != cudaSuccess) return cuda_status(e);
+    if ((rc = flue_multiplymatmat_batch(o, o + 9 * 16, o + 18 * 16, 1, FLUE_C128, 0, c->st))) return rc;
+    return fetch(c, MM, o + 18 * 16, 9 * 16);
+}
+
+int flue_fixsu3matrix_c(double* U_x) {
+    if (!U_x) return fail(FLUE_ERR_ARG, "NULL pointer");
+    HOST_PROLOGUE();
+    if ((rc = grow(&c->out, &c->out_bytes, 2 * 9 * 16))) return rc;
+    char* o = (char*)c->out;
+    cudaError_t e = cudaMemcpyAsync(o, U_x, 9 * 16, cudaMemcpyHostToDevice, c->st);
+    if (e != cudaSuccess) return cuda_status(e);
+    // one 3x3 matrix as a 1-site field with a single direction: strides of
+    // (t,x,y,z,mu,a,b) = (0,0,0,0,0,1,3)
+    const int64_t st[7] = {0, 0, 0, 0, 0, 1, 3};
+    // pack into a 1x1x1x1 C128 field (4 directions, all the same matrix)
+    if ((rc = grow(&c->field2, &c->field2_bytes, 36 * 16))) return rc;
+    if ((rc = flue_pack_field(o, FLUE_C128, st, 1, 1, 1, 1, c->field2, FLUE_C128, 1, c->st))) return rc;
+    // direction 0 of site 0: element (a,b) at 4*(a+3b)
+    double tmp[36 * 2];
+    if ((rc = fetch(c, tmp, c->field2, 36 * 16))) return rc;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            U_x[2 * (a + 3 * b)] = tmp[2 * 4 * (a + 3 * b)];
+            U_x[2 * (a + 3 * b) + 1] = tmp[2 * 4 * (a + 3 * b) + 1];
+        }
+    return FLUE_OK;
+}
+
+int flue_uzerobar_c(const double* data, int NT, int NX, int NY, int NZ, const double* G, double* u0) {
+    if (!u0) return fail(FLUE_ERR_ARG, "NULL output");
+    HOST_PROLOGUE();
+    flue_field U;
+    if ((rc = upload_c128(c, data, NT, NX, NY, NZ, &U))) return rc;
+    if ((rc = ensure_ws(c, FLUE_OP_MEANLINK, U))) return rc;
+    const size_t need2 = flue_workspace_bytes(FLUE_OP_PLAQUETTE, NT, NX, NY, NZ, FLUE_C128);
+    if (need2 > c->ws_bytes && (rc = grow(&c->ws, &c->ws_bytes, need2))) return rc;
+    const int ranges[3][3] = {{1, 4, 4}, {2, 4, 4}, {1, 1, 4}};
+    for (int k = 0; k < 3; ++k)
+        if ((rc = flue_plaquette(&U, ranges[k][0], ranges[k][1], ranges[k][2], c->scal + k, c->ws, c->ws_bytes, c->st)))
+            return rc;
+    if (G) {
+        const size_t gb = (size_t)NT * NX * NY * NZ * 9 * 16;
+        if ((rc = grow(&c->out, &c->out_bytes, gb))) return rc;
+        cudaError_t e = cudaMemcpyAsync(c->out, G, gb, cudaMemcpyHostToDevice, c->st);
+        if (e != cudaSuccess) return cuda_status(e);
+        if ((rc = flue_meanlink(&U, c->out, FLUE_C128, c->scal + 3, c->ws, c->ws_bytes, c->st))) return rc;
+    }
+    double s[7];
+    if ((rc = fetch(c, s, c->scal, 7 * sizeof(double)))) return rc;
+    const double V = (double)NT * NX * NY * NZ;
+    const double p_all = s[0] / (6.0 * V) / 3.0, p_s = s[1] / (3.0 * V) / 3.0, p_t = s[2] / (3.0 * V) / 3.0;
+    u0[0] = pow(p_all, 0.25);
+    u0[1] = pow(p_s, 0.25);
+    u0[2] = sqrt(p_t) / u0[1];
+    if (G) {
+        u0[3] = (s[3] + s[4] + s[5] + s[6]) / (4.0 * V) / 3.0;
+        u0[4] = (s[4] + s[5] + s[6]) / (3.0 * V) / 3.0;
+        u0[5] = s[3] / V / 3.0;
+    } else {
+        u0[3] = u0[4] = u0[5] = NAN;
+    }
+    return FLUE_OK;
+}
+
+int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int NY, int NZ, int prec, int force_form,
+                          double* B, void* grad) {
+    if (!data || !B) return fail(FLUE_ERR_ARG, "NULL pointer");
+    if (data_dtype != FLUE_C128 && data_dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "data must be c128 or c64");
+    if (!prec_ok(prec)) return fail(FLUE_ERR_DTYPE, "bad precision");
+    if ((data_dtype == FLUE_C128) != (prec == FLUE_C128))
+        return fail(FLUE_ERR_DTYPE, "c128 data needs FLUE_C128, c64 data FLUE_C64 or FLUE_R12");
+    if (!dims_ok(NT, NX, NY, NZ)) return fail(FLUE_ERR_SHAPE, "bad lattice extents");
+    HOST_PROLOGUE();
+    const size_t in_bytes = (size_t)flue_field_bytes(NT, NX, NY, NZ, data_dtype);
+    if ((rc = grow(&c->field, &c->field_bytes, in_bytes))) return rc;
+    cudaError_t e = cudaMemcpyAsync(c->field, data, in_bytes, cudaMemcpyHostToDevice, c->st);
+    if (e != cudaSuccess) return cuda_status(e);
+    flue_field U = {c->field, NT, NX, NY, NZ, prec};
+    if (prec == FLUE_R12) {
+        const int64_t V = (int64_t)NT * NX * NY * NZ;
+        const int64_t st[7] = {1, NT, (int64_t)NT * NX, (int64_t)NT * NX * NY, V, 4 * V, 12 * V};
+        if ((rc = grow(&c->field2, &c->field2_bytes, (size_t)flue_field_bytes(NT, NX, NY, NZ, FLUE_R12)))) return rc;
+        if ((rc = flue_pack_field(c->field, FLUE_C64, st, NT, NX, NY, NZ, c->field2, FLUE_R12, 0, c->st))) return rc;
+        U.links = c->field2;
+    }
+    if ((rc = ensure_ws(c, FLUE_OP_MAGNETIC_FORCE, U))) return rc;
+    if (grad && (rc = grow(&c->out, &c->out_bytes, in_bytes))) return rc;
+    if ((rc = flue_magnetic_force(&U, c->scal, grad ? c->out : nullptr, force_form, c->ws, c->ws_bytes, c->st)))
+        return rc;
+    if (grad) {
+        e = cudaMemcpyAsync(grad, c->out, in_bytes, cudaMemcpyDeviceToHost, c->st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
+    return fetch(c, B, c->scal, sizeof(double));
+}
+
+void flue_release_host_cache(void) {
+    std::lock_guard<std::mutex> lk(g_cache_mtx);
+    for (DevCache* c : g_caches) {
+        if (!c) continue;
+        std::lock_guard<std::mutex> lk2(c->mtx);
+        if (c->field) cudaFree(c->field);
+        if (c->field2) cudaFree(c->field2);
+        if (c->ws) cudaFree(c->ws);
+        if (c->out) cudaFree(c->out);
+        c->field = c->field2 = c->ws = c->out = nullptr;
+        c->field_bytes = c->field2_bytes = c->ws_bytes = c->out_bytes = 0;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,534 @@
+// flue_common.cuh -- device-side building blocks shared by every kernel.
+//
+//  * M3<T>: a 3x3 complex matrix held in registers as 9 real + 9 imaginary
+//    parts (row-major, element (a,b) at 3a+b).  T = double for the FP64
+//    path, float for the FP32 path.  The products are the 3x3 complex algebra
+//    of src/SU3MatrixOps.f90 (MultiplyMatMat :19-37, MultiplyMatdagMatdag
+//    :39-58, traces :60-92) written as FMA chains, with the dagger of either
+//    operand folded into the index pattern at compile time.
+//  * Link storage on the device ("field layouts"):
+//      - FULL (complex128 or complex64): exactly the reference's Fortran
+//        array data(NT,NX,NY,NZ,4,3,3) (src/wloops.F90:60): complex element
+//        (s, mu, a, b) at offset s + V*(mu + 4*(a + 3*b)).  Every colour
+//        component is a site-fastest plane, so a warp reading 32 consecutive
+//        sites issues fully coalesced 16-byte (c128) or 8-byte (c64) loads.
+//      - R12 (float): the first two rows only, as three float4 planes per
+//        direction: float4 (mu, k) of site s at s + V*(k + 3*mu), k = 0:
+//        (U00,U01), 1: (U02,U10), 2: (U11,U12).  The third row is rebuilt as
+//        conj(row0 x row1), the vector_product of FixSU3Matrix
+//        (src/gaugeIO/ILDG_bin.f90:120-135, :146).  48 bytes per link with
+//        128-bit coalesced loads.
+//  * Geometry: sites are numbered t-fastest, s = t + NT*(x + NX*(y + NY*z)),
+//    direction index mu = 0,1,2,3 <-> t,x,y,z (the reference's 1..4).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace flue {
+
+enum Prec : int { PREC_C128 = 0, PREC_C64 = 1, PREC_R12 = 2 };
+
+template <typename T>
+struct V2;
+template <>
+struct V2<double> {
+    using type = double2;
+};
+template <>
+struct V2<float> {
+    using type = float2;
+};
+
+template <typename T>
+struct M3 {
+    T r[9], i[9];
+};
+
+template <typename T>
+__device__ __forceinline__ M3<T> m_zero() {
+    M3<T> m;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) m.r[k] = m.i[k] = T(0);
+    return m;
+}
+template <typename T>
+__device__ __forceinline__ M3<T> m_ident() {
+    M3<T> m = m_zero<T>();
+    m.r[0] = m.r[4] = m.r[8] = T(1);
+    return m;
+}
+template <typename T>
+__device__ __forceinline__ M3<T> dag(const M3<T>& a) {
+    M3<T> m;
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int y = 0; y < 3; ++y) {
+            m.r[3 * x + y] = a.r[3 * y + x];
+            m.i[3 * x + y] = -a.i[3 * y + x];
+        }
+    return m;
+}
+template <typename T>
+__device__ __forceinline__ M3<T> transp(const M3<T>& a) {
+    M3<T> m;
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int y = 0; y < 3; ++y) {
+            m.r[3 * x + y] = a.r[3 * y + x];
+            m.i[3 * x + y] = a.i[3 * y + x];
+        }
+    return m;
+}
+
+// C += op(A) * op(B), op = dagger when DA / DB.
+template <bool DA, bool DB, typename T>
+__device__ __forceinline__ void mac(M3<T>& C, const M3<T>& A, const M3<T>& B) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            T re = C.r[3 * a + b], im = C.i[3 * a + b];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T ar = DA ? A.r[3 * k + a] : A.r[3 * a + k];
+                const T ai = DA ? -A.i[3 * k + a] : A.i[3 * a + k];
+                const T br = DB ? B.r[3 * b + k] : B.r[3 * k + b];
+                const T bi = DB ? -B.i[3 * b + k] : B.i[3 * k + b];
+                re = fma(ar, br, re);
+                re = fma(-ai, bi, re);
+                im = fma(ar, bi, im);
+                im = fma(ai, br, im);
+            }
+            C.r[3 * a + b] = re;
+            C.i[3 * a + b] = im;
+        }
+}
+
+// C = op(A) * op(B)
+template <bool DA, bool DB, typename T>
+__device__ __forceinline__ M3<T> mm(const M3<T>& A, const M3<T>& B) {
+    M3<T> C;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const T ar0 = DA ? A.r[a] : A.r[3 * a];
+            const T ai0 = DA ? -A.i[a] : A.i[3 * a];
+            const T br0 = DB ? B.r[3 * b] : B.r[b];
+            const T bi0 = DB ? -B.i[3 * b] : B.i[b];
+            T re = ar0 * br0;
+            T im = ar0 * bi0;
+            re = fma(-ai0, bi0, re);
+            im = fma(ai0, br0, im);
+#pragma unroll
+            for (int k = 1; k < 3; ++k) {
+                const T ar = DA ? A.r[3 * k + a] : A.r[3 * a + k];
+                const T ai = DA ? -A.i[3 * k + a] : A.i[3 * a + k];
+                const T br = DB ? B.r[3 * b + k] : B.r[3 * k + b];
+                const T bi = DB ? -B.i[3 * b + k] : B.i[3 * k + b];
+                re = fma(ar, br, re);
+                re = fma(-ai, bi, re);
+                im = fma(ar, bi, im);
+                im = fma(ai, br, im);
+            }
+            C.r[3 * a + b] = re;
+            C.i[3 * a + b] = im;
+        }
+    return C;
+}
+
+template <typename T>
+__device__ __forceinline__ M3<T> mul(const M3<T>& A, const M3<T>& B) {
+    return mm<false, false>(A, B);
+}
+
+// Re Tr(op(A) op(B))
+template <bool DA, bool DB, typename T>
+__device__ __forceinline__ T retr_mm(const M3<T>& A, const M3<T>& B) {
+    T s = T(0);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const T ar = DA ? A.r[3 * k + a] : A.r[3 * a + k];
+            const T ai = DA ? -A.i[3 * k + a] : A.i[3 * a + k];
+            const T br = DB ? B.r[3 * a + k] : B.r[3 * k + a];
+            const T bi = DB ? -B.i[3 * a + k] : B.i[3 * k + a];
+            s = fma(ar, br, s);
+            s = fma(-ai, bi, s);
+        }
+    return s;
+}
+
+template <typename T>
+__device__ __forceinline__ T retr(const M3<T>& A) {
+    return A.r[0] + A.r[4] + A.r[8];
+}
+
+template <typename T>
+__device__ __forceinline__ void m_add(M3<T>& acc, const M3<T>& b) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        acc.r[k] += b.r[k];
+        acc.i[k] += b.i[k];
+    }
+}
+template <typename T>
+__device__ __forceinline__ void m_axpy(M3<T>& acc, T s, const M3<T>& b) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        acc.r[k] = fma(s, b.r[k], acc.r[k]);
+        acc.i[k] = fma(s, b.i[k], acc.i[k]);
+    }
+}
+// acc += s * b^dagger
+template <typename T>
+__device__ __forceinline__ void m_axpy_dag(M3<T>& acc, T s, const M3<T>& b) {
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int y = 0; y < 3; ++y) {
+            acc.r[3 * x + y] = fma(s, b.r[3 * y + x], acc.r[3 * x + y]);
+            acc.i[3 * x + y] = fma(-s, b.i[3 * y + x], acc.i[3 * x + y]);
+        }
+}
+template <typename T>
+__device__ __forceinline__ M3<T> m_scale(const M3<T>& a, T s) {
+    M3<T> m;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        m.r[k] = a.r[k] * s;
+        m.i[k] = a.i[k] * s;
+    }
+    return m;
+}
+
+// Projection of cloverLoopMuNuCoord / Loop5MuNuCoord (src/wloops.F90:178-190,
+// :411-423): anti-Hermitian, not traceless, times 1/4.
+template <typename T>
+__device__ __forceinline__ M3<T> ah_quarter(const M3<T>& u) {
+    M3<T> f;
+    const T h = T(0.125);  // 0.5 (projection) * 0.25 (factor)
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        f.r[4 * x] = T(0);
+        f.i[4 * x] = u.i[4 * x] * T(0.25);
+    }
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int y = x + 1; y < 3; ++y) {
+            const T cr = (u.r[3 * x + y] - u.r[3 * y + x]) * h;
+            const T ci = (u.i[3 * x + y] + u.i[3 * y + x]) * h;
+            f.r[3 * x + y] = cr;
+            f.i[3 * x + y] = ci;
+            f.r[3 * y + x] = -cr;
+            f.i[3 * y + x] = ci;
+        }
+    return f;
+}
+
+// Traceless anti-Hermitian part times s: s * [(M - M^+)/2 - Tr((M - M^+)/2)/3].
+template <typename T>
+__device__ __forceinline__ M3<T> ta_scaled(const M3<T>& m, T s) {
+    M3<T> g;
+    const T hs = T(0.5) * s;
+    const T tr = (m.i[0] + m.i[4] + m.i[8]) * (T(1) / T(3));
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+        g.r[4 * x] = T(0);
+        g.i[4 * x] = (m.i[4 * x] - tr) * s;
+    }
+#pragma unroll
+    for (int x = 0; x < 3; ++x)
+#pragma unroll
+        for (int y = x + 1; y < 3; ++y) {
+            const T cr = (m.r[3 * x + y] - m.r[3 * y + x]) * hs;
+            const T ci = (m.i[3 * x + y] + m.i[3 * y + x]) * hs;
+            g.r[3 * x + y] = cr;
+            g.i[3 * x + y] = ci;
+            g.r[3 * y + x] = -cr;
+            g.i[3 * y + x] = ci;
+        }
+    return g;
+}
+
+// ---------------------------------------------------------------------------
+// FixSU3Matrix (src/gaugeIO/ILDG_bin.f90:138-151) in FP64 on rows 0 and 1;
+// row 2 becomes conj(row0 x row1) normalised.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fix_su3_rows(double r[3][3], double i[3][3]) {
+    // normalise row 0 (:154-159)
+    double n = sqrt((r[0][0] * r[0][0] + i[0][0] * i[0][0]) + (r[0][1] * r[0][1] + i[0][1] * i[0][1]) +
+                    (r[0][2] * r[0][2] + i[0][2] * i[0][2]));
+    for (int c = 0; c < 3; ++c) {
+        r[0][c] /= n;
+        i[0][c] /= n;
+    }
+    // orthogonalise row 1 against row 0 (:108-118): w -= v * sum(conj(v) w)
+    double dr = 0.0, di = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        dr += r[0][c] * r[1][c] + i[0][c] * i[1][c];
+        di += r[0][c] * i[1][c] - i[0][c] * r[1][c];
+    }
+    for (int c = 0; c < 3; ++c) {
+        const double pr = r[0][c] * dr - i[0][c] * di, pi = r[0][c] * di + i[0][c] * dr;
+        r[1][c] -= pr;
+        i[1][c] -= pi;
+    }
+    n = sqrt((r[1][0] * r[1][0] + i[1][0] * i[1][0]) + (r[1][1] * r[1][1] + i[1][1] * i[1][1]) +
+             (r[1][2] * r[1][2] + i[1][2] * i[1][2]));
+    for (int c = 0; c < 3; ++c) {
+        r[1][c] /= n;
+        i[1][c] /= n;
+    }
+    // row 2 = conj(row0 x row1) (:120-135), normalised
+    for (int c = 0; c < 3; ++c) {
+        const int j = (c + 1) % 3, k = (c + 2) % 3;
+        const double re = (r[0][j] * r[1][k] - i[0][j] * i[1][k]) - (r[0][k] * r[1][j] - i[0][k] * i[1][j]);
+        const double im = (r[0][j] * i[1][k] + i[0][j] * r[1][k]) - (r[0][k] * i[1][j] + i[0][k] * r[1][j]);
+        r[2][c] = re;
+        i[2][c] = -im;
+    }
+    n = sqrt((r[2][0] * r[2][0] + i[2][0] * i[2][0]) + (r[2][1] * r[2][1] + i[2][1] * i[2][1]) +
+             (r[2][2] * r[2][2] + i[2][2] * i[2][2]));
+    for (int c = 0; c < 3; ++c) {
+        r[2][c] /= n;
+        i[2][c] /= n;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Link storage
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 ldg2(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
+
+// Reference layout (complex128 / complex64), read-only.
+template <typename T>
+struct FullLinks {
+    using C2 = typename V2<T>::type;
+    const C2* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ M3<T> load(int64_t s, int mu) const {
+        M3<T> m;
+        const C2* q = p + s + V * mu;
+        const int64_t st = 4 * V;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const C2 v = ldg2(q + st * (a + 3 * b));
+                m.r[3 * a + b] = v.x;
+                m.i[3 * a + b] = v.y;
+            }
+        return m;
+    }
+};
+
+__device__ __forceinline__ void reconstruct_row2(M3<float>& m) {
+    // row2 = conj(row0 x row1)  (vector_product of FixSU3Matrix)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int j = (c + 1) % 3, k = (c + 2) % 3;
+        // v(j) w(k) - v(k) w(j) with v = row0, w = row1
+        const float re = (m.r[j] * m.r[3 + k] - m.i[j] * m.i[3 + k]) - (m.r[k] * m.r[3 + j] - m.i[k] * m.i[3 + j]);
+        const float im = (m.r[j] * m.i[3 + k] + m.i[j] * m.r[3 + k]) - (m.r[k] * m.i[3 + j] + m.i[k] * m.r[3 + j]);
+        m.r[6 + c] = re;
+        m.i[6 + c] = -im;
+    }
+}
+
+struct R12Links {
+    const float4* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ M3<float> load(int64_t s, int mu) const {
+        M3<float> m;
+        const float4* q = p + s + V * (3 * mu);
+        const float4 a = __ldg(q), b = __ldg(q + V), c = __ldg(q + 2 * V);
+        m.r[0] = a.x;
+        m.i[0] = a.y;
+        m.r[1] = a.z;
+        m.i[1] = a.w;
+        m.r[2] = b.x;
+        m.i[2] = b.y;
+        m.r[3] = b.z;
+        m.i[3] = b.w;
+        m.r[4] = c.x;
+        m.i[4] = c.y;
+        m.r[5] = c.z;
+        m.i[5] = c.w;
+        reconstruct_row2(m);
+        return m;
+    }
+};
+
+// Generic matrix planes: matrix k of site s, element e (row-major 3a+b) at
+// base[(k*9 + e)*V + s].  Used for intermediates (lines, cotangents).
+template <typename T>
+struct MatPlanes {
+    using C2 = typename V2<T>::type;
+    C2* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ M3<T> load(int64_t s, int k) const {
+        M3<T> m;
+        const C2* q = p + (int64_t)k * 9 * V + s;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            const C2 v = q[e * V];
+            m.r[e] = v.x;
+            m.i[e] = v.y;
+        }
+        return m;
+    }
+    __device__ __forceinline__ void store(int64_t s, int k, const M3<T>& m) const {
+        C2* q = p + (int64_t)k * 9 * V + s;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            C2 v;
+            v.x = m.r[e];
+            v.y = m.i[e];
+            q[e * V] = v;
+        }
+    }
+};
+
+// Anti-Hermitian matrices stored as 9 reals per site: Im F00, Im F11, Im F22,
+// F01 (re, im), F02 (re, im), F12 (re, im) at base[(k*9 + e)*V + s].
+template <typename T>
+struct AHPlanes {
+    T* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ M3<T> load(int64_t s, int k) const {
+        const T* q = p + (int64_t)k * 9 * V + s;
+        T v[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) v[e] = q[e * V];
+        M3<T> m;
+        m.r[0] = m.r[4] = m.r[8] = T(0);
+        m.i[0] = v[0];
+        m.i[4] = v[1];
+        m.i[8] = v[2];
+        m.r[1] = v[3];
+        m.i[1] = v[4];
+        m.r[3] = -v[3];
+        m.i[3] = v[4];
+        m.r[2] = v[5];
+        m.i[2] = v[6];
+        m.r[6] = -v[5];
+        m.i[6] = v[6];
+        m.r[5] = v[7];
+        m.i[5] = v[8];
+        m.r[7] = -v[7];
+        m.i[7] = v[8];
+        return m;
+    }
+    __device__ __forceinline__ void store(int64_t s, int k, const M3<T>& m) const {
+        T* q = p + (int64_t)k * 9 * V + s;
+        q[0] = m.i[0];
+        q[V] = m.i[4];
+        q[2 * V] = m.i[8];
+        q[3 * V] = m.r[1];
+        q[4 * V] = m.i[1];
+        q[5 * V] = m.r[2];
+        q[6 * V] = m.i[2];
+        q[7 * V] = m.r[5];
+        q[8 * V] = m.i[5];
+    }
+};
+
+// Output in the reference layout (NT,NX,NY,NZ,[4,]3,3): element (s, slot, a, b)
+// at s + V*(slot + nslot*(a + 3b)).  The caller picks transpose on store.
+template <typename T>
+struct RefOut {
+    using C2 = typename V2<T>::type;
+    C2* __restrict__ p;
+    int64_t V;
+    int nslot;
+    __device__ __forceinline__ void store(int64_t s, int slot, const M3<T>& m) const {
+        C2* q = p + s + V * slot;
+        const int64_t st = V * nslot;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                C2 v;
+                v.x = m.r[3 * a + b];
+                v.y = m.i[3 * a + b];
+                q[st * (a + 3 * b)] = v;
+            }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Geometry
+// ---------------------------------------------------------------------------
+struct Geom {
+    int n[4];       // extents: NT, NX, NY, NZ
+    int64_t st[4];  // site strides: 1, NT, NT*NX, NT*NX*NY
+    int64_t V;
+};
+
+__host__ __device__ inline Geom make_geom(int nt, int nx, int ny, int nz) {
+    Geom g;
+    g.n[0] = nt;
+    g.n[1] = nx;
+    g.n[2] = ny;
+    g.n[3] = nz;
+    g.st[0] = 1;
+    g.st[1] = nt;
+    g.st[2] = (int64_t)nt * nx;
+    g.st[3] = (int64_t)nt * nx * ny;
+    g.V = (int64_t)nt * nx * ny * nz;
+    return g;
+}
+
+__device__ __forceinline__ void site_coords(const Geom& g, int64_t s, int c[4]) {
+    int64_t r = s;
+    c[0] = (int)(r % g.n[0]);
+    r /= g.n[0];
+    c[1] = (int)(r % g.n[1]);
+    r /= g.n[1];
+    c[2] = (int)(r % g.n[2]);
+    c[3] = (int)(r / g.n[2]);
+}
+
+// Site offset of a displacement by k (any sign, |k| <= 4*n) along mu from a
+// site whose mu-coordinate is cmu, with periodic wrap.
+__device__ __forceinline__ int64_t disp(const Geom& g, int mu, int cmu, int k) {
+    const int n = g.n[mu];
+    int t = (cmu + k) % n;
+    if (t < 0) t += n;
+    return (int64_t)(t - cmu) * g.st[mu];
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions: every block writes one FP64 partial per output
+// slot; a single-block finisher sums them in index order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum (blockDim.x a multiple of 32, <= 1024); result valid in
+// thread 0.  `sh` must hold 32 doubles.
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        r = lane < nw ? sh[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+}  // namespace flue

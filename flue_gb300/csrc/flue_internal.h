@@ -1,0 +1,64 @@
+// flue_internal.h -- host-side launchers shared between the kernel files and
+// the C-ABI layer (capi.cu).  Every launcher is asynchronous on `stream`,
+// validates nothing (capi.cu does that) and returns a cudaError_t.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "flue_common.cuh"
+
+namespace flue {
+
+struct FieldRef {
+    const void* links;
+    Geom g;
+    int prec;
+};
+
+// reduction finisher: out[j] = sum_i partial[j*nparts + i], j < nout
+cudaError_t launch_finish_sums(const double* partial, int nparts, int nout, double* out, cudaStream_t st,
+                               double scale = 1.0);
+
+// layouts
+cudaError_t launch_pack(const void* src, int src_dtype, const int64_t strides[7], const Geom& g, void* dst, int dst_prec,
+                        int reunitarise, cudaStream_t st);
+cudaError_t launch_unpack(const FieldRef& U, void* dst, int dst_dtype, cudaStream_t st);
+cudaError_t launch_matmul_batch(const void* l, const void* r, void* o, int64_t n, int dtype, int dagger, cudaStream_t st);
+cudaError_t launch_fix_field(void* links, const Geom& g, int prec, cudaStream_t st);
+
+// observables.  Partial-sum scratch `part` needs partial_slots(...) doubles.
+int plaquette_blocks(const Geom& g);
+cudaError_t launch_plaquette(const FieldRef& U, int mu0, int mu1, int nu1, double* part, double* out, cudaStream_t st);
+int polyakov_blocks(const Geom& g);
+cudaError_t launch_polyakov(const FieldRef& U, double* part, double* out2, cudaStream_t st);
+int wloop_blocks(const Geom& g);
+cudaError_t launch_wloop(const FieldRef& U, int tau, int mu, int nu, int nmu, int nnu, double* part, double* out,
+                         cudaStream_t st);
+cudaError_t launch_genericpath(const FieldRef& U, const int* path_host, int npath, const int* coord_host, void* out,
+                               cudaStream_t st);
+int meanlink_blocks(const Geom& g);
+cudaError_t launch_meanlink(const FieldRef& U, const void* G, int g_dtype, double* part, double* out4, cudaStream_t st);
+
+// field strength / energies (fmunu.cu, force.cu)
+struct PlaneSet {
+    int np;
+    int mu[6], nu[6];  // 0-based directions
+};
+size_t energy_ws_bytes(const Geom& g, int prec, const PlaneSet& ps, bool with_force);
+cudaError_t launch_fmunu(const FieldRef& U, int kind, int mu, int nu, void* out, void* ws, size_t ws_bytes,
+                         cudaStream_t st);
+cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int force_form, void* ws,
+                          size_t ws_bytes, cudaStream_t st);
+int plaqforce_blocks(const Geom& g);
+cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_S, void* force, int force_form,
+                                   cudaStream_t st);
+
+cudaError_t stage_timing_enable(int on);
+cudaError_t stage_times(double* ms, int maxn, int* n);
+
+// Wilson flow (flow.cu)
+size_t wflow_ws_bytes(const Geom& g);
+cudaError_t launch_wflow_step(void* links, const Geom& g, int prec, double eps, void* ws, cudaStream_t st);
+
+}  // namespace flue

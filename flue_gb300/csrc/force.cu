@@ -1,0 +1,507 @@
+// force.cu -- clover and 5-loop F_munu, the 5-loop energy / B^2 and its
+// su(3) gradient, and the Wilson plaquette-action force.
+//
+// The 5-loop field strength (src/wloops.F90:201-432, hep-lat/0203008) at a
+// site x and plane (mu,nu) is built from the 28 counter-clockwise leaves of
+// the rectangles of shapes (a,b) in {(1,1),(2,2),(3,3),(1,2),(2,1),(1,3),(3,1)}
+// (a links along mu, b along nu) that have x as a corner.  The reference walks
+// every leaf link by link (208 link steps and 180 products per plane-site);
+// here a leaf is the product of four straight "lines"
+//     L^a_mu(y) = U_mu(y) U_mu(y+mu) ... U_mu(y+(a-1)mu),   a = 1,2,3,
+// precomputed once per site (2 products per direction), so a leaf costs 3
+// products (84 per plane-site).  Writing the rectangle anchored at y0 (its
+// lower-left corner) as the sides
+//     S1 = L^a_mu(y0),  S2 = L^b_nu(y0+a mu),  S3 = L^a_mu(y0+b nu)^+,  S4 = L^b_nu(y0)^+
+// with corners K1..K4 at y0, y0+a mu, y0+a mu+b nu, y0+b nu, the leaf of x in
+// quadrant q is the cyclic word S_q S_q+1 S_q+2 S_q+3 of the rectangle that
+// has x as its corner q.  genericPath returns the transpose of every leaf
+// (:56); the kernels work with untransposed leaves and transpose on output.
+//
+// Energy E = -1/V sum_x sum_planes Re Tr(F F) (B^2 for the three spatial
+// planes (3,2),(2,4),(4,3) of magnetic, :502-506).  Reverse mode, written as
+// gathers so that no atomics are needed and results are deterministic:
+//   1. lines:   L^2, L^3 per direction                    (k_lines)
+//   2. forward: Q, F = AH(Q)/4, E partials; F kept as the cotangent
+//               dE/dQ = -F/(2V) (stored as 9 reals)        (k_fwd)
+//   3. line cotangents: Lambda^a_d(y) with dE = Re Tr(dL Lambda), summed over
+//      every rectangle side that is the line (y,d,a); each side collects the
+//      four corner insertions K S S S + S K S S + S S K S + S S S K with a
+//      Horner scheme (8 products)                          (k_linecot)
+//   4. link cotangents N_d(z) from the line cotangents of the lines through
+//      the link, then the su(3)-projected gradient G = -1/2 TA(U N) or the
+//      Euclidean gradient N^+                              (k_linkcot)
+#include "flue_internal.h"
+
+namespace flue {
+
+#define FLUE_DISPATCH_LINKS(U, ...)                                              \
+    do {                                                                         \
+        if ((U).prec == PREC_C128) {                                             \
+            using T = double;                                                    \
+            FullLinks<double> L{(const double2*)(U).links, (U).g.V};             \
+            __VA_ARGS__;                                                         \
+        } else if ((U).prec == PREC_C64) {                                       \
+            using T = float;                                                     \
+            FullLinks<float> L{(const float2*)(U).links, (U).g.V};               \
+            __VA_ARGS__;                                                         \
+        } else {                                                                 \
+            using T = float;                                                     \
+            R12Links L{(const float4*)(U).links, (U).g.V};                       \
+            __VA_ARGS__;                                                         \
+        }                                                                        \
+    } while (0)
+
+// 5-loop coefficients, src/wloops.F90:219-224 (k5 = 1/180).
+constexpr double K5c = 1.0 / 180.0;
+constexpr double K1c = (19.0 / 9.0) - 55.0 * K5c;
+constexpr double K2c = (1.0 / 36.0) - 16.0 * K5c;
+constexpr double K3c = 64.0 * K5c - (32.0 / 45.0);
+constexpr double K4c = (1.0 / 15.0) - 6.0 * K5c;
+
+struct Shape {
+    int a, b;
+    double c;
+};
+// kind 1: 5-loop (weights of :327, :341, :358, :382, :405); kind 0: clover.
+__constant__ Shape c_shapes5[7] = {{1, 1, K1c},       {2, 2, K2c},       {3, 3, K5c},      {1, 2, 0.5 * K3c},
+                                   {2, 1, 0.5 * K3c}, {1, 3, 0.5 * K4c}, {3, 1, 0.5 * K4c}};
+__constant__ Shape c_shapes1[1] = {{1, 1, 1.0}};
+
+// Planes and direction slots of one energy evaluation.
+struct PlaneArg {
+    int np;
+    int mu[6], nu[6];
+    int nd;
+    int slot[4];  // direction -> slot, -1 if unused
+    int dir[4];   // slot -> direction
+};
+
+// periodic displacement by k along mu from coordinate cmu (any k)
+__device__ __forceinline__ int64_t dsp(const Geom& g, int mu, int cmu, int k) {
+    const int n = g.n[mu];
+    int t = cmu + k;
+    while (t < 0) t += n;
+    while (t >= n) t -= n;
+    return (int64_t)(t - cmu) * g.st[mu];
+}
+
+template <class L, typename T>
+struct Ctx {
+    L U;
+    MatPlanes<T> lines;  // 2 per slot: L^2, L^3
+    Geom g;
+    int64_t s;
+    int c[4];
+    int mu, nu, smu, snu;  // plane directions and their slots
+    __device__ __forceinline__ int64_t at(int i, int j) const {
+        return s + dsp(g, mu, c[mu], i) + dsp(g, nu, c[nu], j);
+    }
+    __device__ __forceinline__ M3<T> line(int dir, int slot, int len, int64_t site) const {
+        if (len == 1) return U.load(site, dir);
+        return lines.load(site, 2 * slot + len - 2);
+    }
+    // side k (1..4) of the rectangle anchored at (i0,j0) with shape (a,b)
+    __device__ __forceinline__ M3<T> side(int k, int i0, int j0, int a, int b) const {
+        switch (k) {
+            case 1:
+                return line(mu, smu, a, at(i0, j0));
+            case 2:
+                return line(nu, snu, b, at(i0 + a, j0));
+            case 3:
+                return dag(line(mu, smu, a, at(i0, j0 + b)));
+            default:
+                return dag(line(nu, snu, b, at(i0, j0)));
+        }
+    }
+};
+
+__device__ __forceinline__ void corner_off(int k, int a, int b, int& di, int& dj) {
+    di = (k == 2 || k == 3) ? a : 0;
+    dj = (k == 3 || k == 4) ? b : 0;
+}
+
+// ---------------------------------------------------------------------------
+// 1. lines: L^2_d(y) = U_d(y) U_d(y+d), L^3_d(y) = L^2_d(y) U_d(y+2d)
+// ---------------------------------------------------------------------------
+template <class L, typename T>
+__global__ void k_lines(L U, Geom g, PlaneArg pa, MatPlanes<T> lines) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.V) return;
+    const int slot = blockIdx.y;
+    const int d = pa.dir[slot];
+    int c[4];
+    site_coords(g, s, c);
+    const int64_t s1 = s + dsp(g, d, c[d], 1);
+    const int64_t s2 = s + dsp(g, d, c[d], 2);
+    const M3<T> l2 = mul(U.load(s, d), U.load(s1, d));
+    lines.store(s, 2 * slot, l2);
+    lines.store(s, 2 * slot + 1, mul(l2, U.load(s2, d)));
+}
+
+// ---------------------------------------------------------------------------
+// 2. forward: one thread per (site, plane)
+// ---------------------------------------------------------------------------
+constexpr int FWD_BS = 128;
+
+template <class L, typename T>
+__global__ void __launch_bounds__(FWD_BS)
+    k_fwd(L U, Geom g, PlaneArg pa, int kind, MatPlanes<T> lines, AHPlanes<T> kout, RefOut<T> fout, double* part) {
+    __shared__ double sh[32];
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.y;
+    double e = 0.0;
+    if (s < g.V) {
+        Ctx<L, T> cx{U, lines, g, s, {0, 0, 0, 0}, pa.mu[p], pa.nu[p], pa.slot[pa.mu[p]], pa.slot[pa.nu[p]]};
+        site_coords(g, s, cx.c);
+        const Shape* shp = kind == 1 ? c_shapes5 : c_shapes1;
+        const int nsh = kind == 1 ? 7 : 1;
+        M3<T> q = m_zero<T>();
+        for (int k = 0; k < nsh; ++k) {
+            const int a = shp[k].a, b = shp[k].b;
+            M3<T> w = m_zero<T>();
+            for (int qd = 1; qd <= 4; ++qd) {
+                int di, dj;
+                corner_off(qd, a, b, di, dj);
+                const int i0 = -di, j0 = -dj;
+                const M3<T> s0 = cx.side(qd, i0, j0, a, b);
+                const M3<T> s1 = cx.side(qd % 4 + 1, i0, j0, a, b);
+                const M3<T> t01 = mul(s0, s1);
+                const M3<T> s2 = cx.side((qd + 1) % 4 + 1, i0, j0, a, b);
+                const M3<T> t012 = mul(t01, s2);
+                const M3<T> s3 = cx.side((qd + 2) % 4 + 1, i0, j0, a, b);
+                mac<false, false>(w, t012, s3);
+            }
+            m_axpy(q, (T)shp[k].c, w);
+        }
+        const M3<T> f = ah_quarter(q);
+        e = -(double)retr_mm<false, false>(f, f);
+        if (kout.p) kout.store(s, p, f);
+        if (fout.p) fout.store(s, 0, transp(f));
+    }
+    if (part) {
+        const double r = block_sum(e, sh);
+        if (threadIdx.x == 0) part[(int64_t)p * gridDim.x + blockIdx.x] = r;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. line cotangents: one thread per (site, slot, length)
+// ---------------------------------------------------------------------------
+constexpr int COT_BS = 128;
+
+template <class L, typename T>
+__device__ __forceinline__ M3<T> corner_k(const Ctx<L, T>& cx, const AHPlanes<T>& kin, int p, int k, int i0, int j0, int a,
+                                          int b) {
+    int di, dj;
+    corner_off(k, a, b, di, dj);
+    return kin.load(cx.at(i0 + di, j0 + dj), p);
+}
+
+// Sum of the four corner insertions in the word that follows side q of the
+// rectangle (i0,j0,a,b):  Ka A B C + A Kb B C + A B Kc C + A B C Kd with
+// A,B,C = S_q+1, S_q+2, S_q+3 and Ka,Kb,Kc,Kd = K_q+1, K_q+2, K_q+3, K_q.
+template <class L, typename T>
+__device__ __forceinline__ M3<T> side_cot(const Ctx<L, T>& cx, const AHPlanes<T>& kin, int p, int q, int i0, int j0, int a,
+                                          int b) {
+    const int q1 = q % 4 + 1, q2 = q1 % 4 + 1, q3 = q2 % 4 + 1;
+    const M3<T> C = cx.side(q3, i0, j0, a, b);
+    M3<T> t1;
+    {
+        const M3<T> kd = corner_k(cx, kin, p, q, i0, j0, a, b);
+        t1 = mul(C, kd);
+        const M3<T> kc = corner_k(cx, kin, p, q3, i0, j0, a, b);
+        mac<false, false>(t1, kc, C);
+    }
+    const M3<T> B = cx.side(q2, i0, j0, a, b);
+    const M3<T> bc = mul(B, C);
+    M3<T> t2 = mul(B, t1);
+    {
+        const M3<T> kb = corner_k(cx, kin, p, q2, i0, j0, a, b);
+        mac<false, false>(t2, kb, bc);
+    }
+    const M3<T> A = cx.side(q1, i0, j0, a, b);
+    const M3<T> abc = mul(A, bc);
+    M3<T> res = mul(A, t2);
+    {
+        const M3<T> ka = corner_k(cx, kin, p, q1, i0, j0, a, b);
+        mac<false, false>(res, ka, abc);
+    }
+    return res;
+}
+
+template <class L, typename T>
+__global__ void __launch_bounds__(COT_BS)
+    k_linecot(L U, Geom g, PlaneArg pa, MatPlanes<T> lines, AHPlanes<T> kin, MatPlanes<T> lam) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.V) return;
+    const int slot = blockIdx.y / 3;
+    const int len = blockIdx.y % 3 + 1;
+    const int d = pa.dir[slot];
+    int c[4];
+    site_coords(g, s, c);
+    M3<T> acc = m_zero<T>();
+    for (int p = 0; p < pa.np; ++p) {
+        const bool is_mu = pa.mu[p] == d, is_nu = pa.nu[p] == d;
+        if (!is_mu && !is_nu) continue;
+        Ctx<L, T> cx{U, lines, g, s, {c[0], c[1], c[2], c[3]}, pa.mu[p], pa.nu[p], pa.slot[pa.mu[p]], pa.slot[pa.nu[p]]};
+        for (int k = 0; k < 7; ++k) {
+            const int a = c_shapes5[k].a, b = c_shapes5[k].b;
+            const T coef = (T)c_shapes5[k].c;
+            if (is_mu && a == len) {
+                // the line is S1 of the rectangle anchored here ...
+                m_axpy(acc, coef, side_cot(cx, kin, p, 1, 0, 0, a, b));
+                // ... and S3 (daggered) of the one anchored b below.
+                m_axpy_dag(acc, coef, side_cot(cx, kin, p, 3, 0, -b, a, b));
+            }
+            if (is_nu && b == len) {
+                // S2 of the rectangle anchored a to the left ...
+                m_axpy(acc, coef, side_cot(cx, kin, p, 2, -a, 0, a, b));
+                // ... and S4 (daggered) of the one anchored here.
+                m_axpy_dag(acc, coef, side_cot(cx, kin, p, 4, 0, 0, a, b));
+            }
+        }
+    }
+    lam.store(s, 3 * slot + len - 1, acc);
+}
+
+// ---------------------------------------------------------------------------
+// 4. link cotangents and gradient output: one thread per (site, direction)
+// ---------------------------------------------------------------------------
+template <class L, typename T>
+__global__ void k_linkcot(L U, Geom g, PlaneArg pa, MatPlanes<T> lines, MatPlanes<T> lam, T scale, int form,
+                          RefOut<T> out) {
+    const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= g.V) return;
+    const int d = blockIdx.y;
+    const int slot = pa.slot[d];
+    if (slot < 0) {
+        out.store(z, d, m_zero<T>());
+        return;
+    }
+    int c[4];
+    site_coords(g, z, c);
+    const int64_t zp = z + dsp(g, d, c[d], 1), zm = z + dsp(g, d, c[d], -1), zmm = z + dsp(g, d, c[d], -2);
+    const M3<T> up = U.load(zp, d);
+    const M3<T> um = U.load(zm, d);
+    M3<T> n = lam.load(z, 3 * slot);
+    mac<false, false>(n, up, lam.load(z, 3 * slot + 1));
+    mac<false, false>(n, lam.load(zm, 3 * slot + 1), um);
+    mac<false, false>(n, lines.load(zp, 2 * slot), lam.load(z, 3 * slot + 2));
+    {
+        const M3<T> t = mul(up, lam.load(zm, 3 * slot + 2));
+        mac<false, false>(n, t, um);
+    }
+    mac<false, false>(n, lam.load(zmm, 3 * slot + 2), lines.load(zmm, 2 * slot));
+    if (form == 0) {
+        const M3<T> un = mul(U.load(z, d), n);
+        out.store(z, d, ta_scaled(un, T(-0.5) * scale));
+    } else {
+        out.store(z, d, m_scale(dag(n), scale));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static PlaneArg make_planes(const PlaneSet& ps) {
+    PlaneArg pa;
+    pa.np = ps.np;
+    for (int k = 0; k < 4; ++k) pa.slot[k] = -1, pa.dir[k] = -1;
+    pa.nd = 0;
+    for (int p = 0; p < ps.np; ++p) {
+        pa.mu[p] = ps.mu[p];
+        pa.nu[p] = ps.nu[p];
+        for (int d : {ps.mu[p], ps.nu[p]})
+            if (pa.slot[d] < 0) {
+                pa.slot[d] = pa.nd;
+                pa.dir[pa.nd] = d;
+                pa.nd++;
+            }
+    }
+    return pa;
+}
+
+static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct EnergyWs {
+    size_t lines, kbuf, lam, part, total;
+};
+
+static EnergyWs energy_layout(const Geom& g, int prec, const PlaneArg& pa, bool with_force) {
+    const size_t cs = prec == PREC_C128 ? 8 : 4;  // real size of compute type
+    EnergyWs w;
+    const int nbx = (int)((g.V + FWD_BS - 1) / FWD_BS);
+    w.lines = 0;
+    w.kbuf = align256(w.lines + (size_t)2 * pa.nd * 9 * g.V * 2 * cs);
+    w.lam = align256(w.kbuf + (with_force ? (size_t)pa.np * 9 * g.V * cs : 0));
+    w.part = align256(w.lam + (with_force ? (size_t)3 * pa.nd * 9 * g.V * 2 * cs : 0));
+    w.total = align256(w.part + (size_t)pa.np * nbx * sizeof(double));
+    return w;
+}
+
+size_t energy_ws_bytes(const Geom& g, int prec, const PlaneSet& ps, bool with_force) {
+    return energy_layout(g, prec, make_planes(ps), with_force).total;
+}
+
+// Optional per-stage timing of the energy pipeline (CUDA events recorded on
+// the caller's stream between the stage launches): stage 0 lines, 1 forward
+// (+ sum), 2 line cotangents, 3 link cotangents.
+static bool g_stage_on = false;
+static cudaEvent_t g_stage_ev[5] = {};
+static int g_stage_n = 0;
+
+cudaError_t stage_timing_enable(int on) {
+    if (on && !g_stage_ev[0]) {
+        for (auto& e : g_stage_ev) {
+            cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess) return r;
+        }
+    }
+    g_stage_on = on != 0;
+    g_stage_n = 0;
+    return cudaSuccess;
+}
+
+cudaError_t stage_times(double* ms, int maxn, int* n) {
+    *n = 0;
+    if (!g_stage_on || g_stage_n < 2) return cudaSuccess;
+    cudaError_t r = cudaEventSynchronize(g_stage_ev[g_stage_n - 1]);
+    if (r != cudaSuccess) return r;
+    for (int k = 0; k + 1 < g_stage_n && k < maxn; ++k) {
+        float t = 0.f;
+        r = cudaEventElapsedTime(&t, g_stage_ev[k], g_stage_ev[k + 1]);
+        if (r != cudaSuccess) return r;
+        ms[k] = t;
+        *n = k + 1;
+    }
+    return cudaSuccess;
+}
+
+static inline void stage_mark(int k, cudaStream_t st) {
+    if (g_stage_on) {
+        cudaEventRecord(g_stage_ev[k], st);
+        g_stage_n = k + 1;
+    }
+}
+
+template <class L, typename T>
+static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, int kind, double* out_E, void* force,
+                               int form, char* ws, const EnergyWs& w, RefOut<T> fout, cudaStream_t st) {
+    using C2 = typename V2<T>::type;
+    MatPlanes<T> lines{(C2*)(ws + w.lines), g.V};
+    AHPlanes<T> kb{force ? (T*)(ws + w.kbuf) : nullptr, g.V};
+    MatPlanes<T> lam{(C2*)(ws + w.lam), g.V};
+    double* part = out_E ? (double*)(ws + w.part) : nullptr;
+    const unsigned nbx = (unsigned)((g.V + FWD_BS - 1) / FWD_BS);
+    stage_mark(0, st);
+    k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, pa, lines);
+    stage_mark(1, st);
+    k_fwd<L, T><<<dim3(nbx, pa.np), FWD_BS, 0, st>>>(U, g, pa, kind, lines, kb, fout, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (out_E) {
+        e = launch_finish_sums(part, (int)(nbx * pa.np), 1, out_E, st);
+        if (e != cudaSuccess) return e;
+    }
+    stage_mark(2, st);
+    if (!force) return cudaSuccess;
+    const unsigned nbc = (unsigned)((g.V + COT_BS - 1) / COT_BS);
+    k_linecot<L, T><<<dim3(nbc, 3 * pa.nd), COT_BS, 0, st>>>(U, g, pa, lines, kb, lam);
+    stage_mark(3, st);
+    RefOut<T> fo{(C2*)force, g.V, 4};
+    const T scale = (T)(-1.0 / (2.0 * (double)g.V));
+    k_linkcot<L, T><<<dim3((unsigned)((g.V + 127) / 128), 4), 128, 0, st>>>(U, g, pa, lines, lam, scale, form, fo);
+    stage_mark(4, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int force_form, void* ws,
+                          size_t ws_bytes, cudaStream_t st) {
+    const PlaneArg pa = make_planes(ps);
+    const EnergyWs w = energy_layout(U.g, U.prec, pa, force != nullptr);
+    if (ws_bytes < w.total) return cudaErrorInvalidValue;
+    FLUE_DISPATCH_LINKS(U, {
+        RefOut<T> none{nullptr, U.g.V, 1};
+        return energy_impl<decltype(L), T>(L, U.g, pa, 1, out_E, force, force_form, (char*)ws, w, none, st);
+    });
+    return cudaSuccess;
+}
+
+// F_munu of one plane: kind 0 = clover (cloverLoopMuNuCoord), 1 = 5-loop
+// (Loop5MuNuCoord).  Output (NT,NX,NY,NZ,3,3) in the field's compute dtype.
+cudaError_t launch_fmunu(const FieldRef& U, int kind, int mu, int nu, void* out, void* ws, size_t ws_bytes,
+                         cudaStream_t st) {
+    PlaneSet ps;
+    ps.np = 1;
+    ps.mu[0] = mu;
+    ps.nu[0] = nu;
+    const PlaneArg pa = make_planes(ps);
+    const EnergyWs w = energy_layout(U.g, U.prec, pa, false);
+    if (ws_bytes < w.total) return cudaErrorInvalidValue;
+    FLUE_DISPATCH_LINKS(U, {
+        using C2 = typename V2<T>::type;
+        RefOut<T> fo{(C2*)out, U.g.V, 1};
+        return energy_impl<decltype(L), T>(L, U.g, pa, kind, nullptr, nullptr, 0, (char*)ws, w, fo, st);
+    });
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// Wilson plaquette action S = sum_{x,mu<nu} Re Tr P_munu(x) and its gradient:
+// N_mu(x) = sum_{nu != mu} [U_nu(x+mu) U_mu(x+nu)^+ U_nu(x)^+
+//                           + U_nu(x+mu-nu)^+ U_mu(x-nu)^+ U_nu(x-nu)]
+// ---------------------------------------------------------------------------
+constexpr int PF_BS = 128;
+int plaqforce_blocks(const Geom& g) { return (int)((g.V + PF_BS - 1) / PF_BS); }
+
+template <class L, typename T>
+__global__ void __launch_bounds__(PF_BS) k_plaqforce(L U, Geom g, int form, RefOut<T> out, double* part) {
+    __shared__ double sh[32];
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int mu = blockIdx.y;
+    double acc = 0.0;
+    if (s < g.V) {
+        int c[4];
+        site_coords(g, s, c);
+        const int64_t sp = s + dsp(g, mu, c[mu], 1);
+        const M3<T> u = U.load(s, mu);
+        M3<T> n = m_zero<T>();
+        for (int nu = 0; nu < 4; ++nu) {
+            if (nu == mu) continue;
+            const int64_t sn = s + dsp(g, nu, c[nu], 1);
+            const int64_t sm = s + dsp(g, nu, c[nu], -1);
+            const int64_t spm = sp + dsp(g, nu, c[nu], -1);
+            const M3<T> up = mm<false, true>(U.load(sp, nu), U.load(sn, mu));
+            const M3<T> upper = mm<false, true>(up, U.load(s, nu));
+            if (nu > mu) acc += (double)retr_mm<false, false>(u, upper);
+            m_add(n, upper);
+            const M3<T> dn = mm<true, true>(U.load(spm, nu), U.load(sm, mu));
+            mac<false, false>(n, dn, U.load(sm, nu));
+        }
+        if (out.p) {
+            if (form == 0)
+                out.store(s, mu, ta_scaled(mul(u, n), T(-0.5)));
+            else
+                out.store(s, mu, dag(n));
+        }
+    }
+    if (part) {
+        const double r = block_sum(acc, sh);
+        if (threadIdx.x == 0) part[(int64_t)mu * gridDim.x + blockIdx.x] = r;
+    }
+}
+
+cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_S, void* force, int force_form,
+                                   cudaStream_t st) {
+    const int nb = plaqforce_blocks(U.g);
+    FLUE_DISPATCH_LINKS(U, {
+        using C2 = typename V2<T>::type;
+        RefOut<T> fo{(C2*)force, U.g.V, 4};
+        k_plaqforce<decltype(L), T><<<dim3(nb, 4), PF_BS, 0, st>>>(L, U.g, force_form, fo, out_S ? part : nullptr);
+    });
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !out_S) return e;
+    return launch_finish_sums(part, 4 * nb, 1, out_S, st);
+}
+
+}  // namespace flue

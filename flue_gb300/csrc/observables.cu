@@ -1,0 +1,476 @@
+// observables.cu -- layout conversion, SU(3) batch products, and the scalar
+// observables of src/wloops.F90: plaquette (:915-1017, same observable as
+// genPlaquette :59-127), polyakov (:1019-1069), wmunu / wmunutau
+// (:567-791), genericPath (:20-57) and the Landau-gauge mean link used by
+// uzerobar.  Every scalar is accumulated per thread in FP64 (the FP32 path
+// computes link products in FP32 and converts each per-site trace), reduced
+// per block with warp shuffles, and finished by a one-block kernel that adds
+// the block partials in index order, so results are bitwise reproducible for
+// a given lattice size.
+#include "flue_internal.h"
+
+namespace flue {
+
+// ---------------------------------------------------------------------------
+// precision dispatch
+// ---------------------------------------------------------------------------
+#define FLUE_DISPATCH_LINKS(U, ...)                                              \
+    do {                                                                         \
+        if ((U).prec == PREC_C128) {                                             \
+            using T = double;                                                    \
+            FullLinks<double> L{(const double2*)(U).links, (U).g.V};             \
+            __VA_ARGS__;                                                         \
+        } else if ((U).prec == PREC_C64) {                                       \
+            using T = float;                                                     \
+            FullLinks<float> L{(const float2*)(U).links, (U).g.V};               \
+            __VA_ARGS__;                                                         \
+        } else {                                                                 \
+            using T = float;                                                     \
+            R12Links L{(const float4*)(U).links, (U).g.V};                       \
+            __VA_ARGS__;                                                         \
+        }                                                                        \
+    } while (0)
+
+static inline int grid_for(int64_t n, int bs, int cap) {
+    int64_t b = (n + bs - 1) / bs;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// ---------------------------------------------------------------------------
+// reduction finisher
+// ---------------------------------------------------------------------------
+__global__ void k_finish_sums(const double* __restrict__ part, int nparts, double scale, double* __restrict__ out) {
+    __shared__ double sh[32];
+    const double* p = part + (int64_t)blockIdx.x * nparts;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += p[i];
+    double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) out[blockIdx.x] = scale == 1.0 ? r : r * scale;
+}
+
+cudaError_t launch_finish_sums(const double* partial, int nparts, int nout, double* out, cudaStream_t st, double scale) {
+    k_finish_sums<<<nout, 256, 0, st>>>(partial, nparts, scale, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// pack: arbitrary-strided (t,x,y,z,mu,a,b) complex128/complex64 -> device
+// layout, optionally reunitarised.  One thread per (site, mu).
+// ---------------------------------------------------------------------------
+struct Strides7 {
+    int64_t s[7];
+};
+
+template <typename SRC>
+__global__ void k_pack(const SRC* __restrict__ src, Strides7 sd, Geom g, void* __restrict__ dst, int dst_prec, int reun) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 4 * g.V) return;
+    const int64_t s = idx % g.V;
+    const int mu = (int)(idx / g.V);
+    int c[4];
+    site_coords(g, s, c);
+    const int64_t base = c[0] * sd.s[0] + c[1] * sd.s[1] + c[2] * sd.s[2] + c[3] * sd.s[3] + mu * sd.s[4];
+    double r[3][3], im[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            const SRC v = src[base + a * sd.s[5] + b * sd.s[6]];
+            r[a][b] = (double)v.x;
+            im[a][b] = (double)v.y;
+        }
+    if (reun) fix_su3_rows(r, im);
+    if (dst_prec == PREC_C128) {
+        double2* o = (double2*)dst + s + g.V * mu;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) o[4 * g.V * (a + 3 * b)] = make_double2(r[a][b], im[a][b]);
+    } else if (dst_prec == PREC_C64) {
+        float2* o = (float2*)dst + s + g.V * mu;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) o[4 * g.V * (a + 3 * b)] = make_float2((float)r[a][b], (float)im[a][b]);
+    } else {
+        float4* o = (float4*)dst + s + g.V * (3 * mu);
+        o[0] = make_float4((float)r[0][0], (float)im[0][0], (float)r[0][1], (float)im[0][1]);
+        o[g.V] = make_float4((float)r[0][2], (float)im[0][2], (float)r[1][0], (float)im[1][0]);
+        o[2 * g.V] = make_float4((float)r[1][1], (float)im[1][1], (float)r[1][2], (float)im[1][2]);
+    }
+}
+
+cudaError_t launch_pack(const void* src, int src_dtype, const int64_t strides[7], const Geom& g, void* dst, int dst_prec,
+                        int reunitarise, cudaStream_t st) {
+    Strides7 sd;
+    for (int k = 0; k < 7; ++k) sd.s[k] = strides[k];
+    const int64_t n = 4 * g.V;
+    const int bs = 256;
+    const unsigned nb = (unsigned)((n + bs - 1) / bs);
+    if (src_dtype == PREC_C128)
+        k_pack<double2><<<nb, bs, 0, st>>>((const double2*)src, sd, g, dst, dst_prec, reunitarise);
+    else
+        k_pack<float2><<<nb, bs, 0, st>>>((const float2*)src, sd, g, dst, dst_prec, reunitarise);
+    return cudaGetLastError();
+}
+
+// in-place FixSU3Matrix of a device field (any precision)
+__global__ void k_fix_field(void* links, Geom g, int prec) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 4 * g.V) return;
+    const int64_t s = idx % g.V;
+    const int mu = (int)(idx / g.V);
+    double r[3][3], im[3][3];
+    if (prec == PREC_C128) {
+        double2* o = (double2*)links + s + g.V * mu;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const double2 v = o[4 * g.V * (a + 3 * b)];
+                r[a][b] = v.x;
+                im[a][b] = v.y;
+            }
+        fix_su3_rows(r, im);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) o[4 * g.V * (a + 3 * b)] = make_double2(r[a][b], im[a][b]);
+    } else if (prec == PREC_C64) {
+        float2* o = (float2*)links + s + g.V * mu;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const float2 v = o[4 * g.V * (a + 3 * b)];
+                r[a][b] = v.x;
+                im[a][b] = v.y;
+            }
+        fix_su3_rows(r, im);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) o[4 * g.V * (a + 3 * b)] = make_float2((float)r[a][b], (float)im[a][b]);
+    } else {
+        float4* o = (float4*)links + s + g.V * (3 * mu);
+        const float4 q0 = o[0], q1 = o[g.V], q2 = o[2 * g.V];
+        r[0][0] = q0.x; im[0][0] = q0.y; r[0][1] = q0.z; im[0][1] = q0.w;
+        r[0][2] = q1.x; im[0][2] = q1.y; r[1][0] = q1.z; im[1][0] = q1.w;
+        r[1][1] = q2.x; im[1][1] = q2.y; r[1][2] = q2.z; im[1][2] = q2.w;
+        fix_su3_rows(r, im);
+        o[0] = make_float4((float)r[0][0], (float)im[0][0], (float)r[0][1], (float)im[0][1]);
+        o[g.V] = make_float4((float)r[0][2], (float)im[0][2], (float)r[1][0], (float)im[1][0]);
+        o[2 * g.V] = make_float4((float)r[1][1], (float)im[1][1], (float)r[1][2], (float)im[1][2]);
+    }
+}
+
+cudaError_t launch_fix_field(void* links, const Geom& g, int prec, cudaStream_t st) {
+    const int64_t n = 4 * g.V;
+    k_fix_field<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(links, g, prec);
+    return cudaGetLastError();
+}
+
+// unpack: device layout -> reference layout (complex128 or complex64)
+template <class L, typename T, typename D2>
+__global__ void k_unpack(L U, Geom g, D2* __restrict__ dst) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 4 * g.V) return;
+    const int64_t s = idx % g.V;
+    const int mu = (int)(idx / g.V);
+    const M3<T> m = U.load(s, mu);
+    D2* o = dst + s + g.V * mu;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            D2 v;
+            v.x = m.r[3 * a + b];
+            v.y = m.i[3 * a + b];
+            o[4 * g.V * (a + 3 * b)] = v;
+        }
+}
+
+cudaError_t launch_unpack(const FieldRef& U, void* dst, int dst_dtype, cudaStream_t st) {
+    const int64_t n = 4 * U.g.V;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    FLUE_DISPATCH_LINKS(U, {
+        if (dst_dtype == PREC_C128)
+            k_unpack<decltype(L), T, double2><<<nb, 256, 0, st>>>(L, U.g, (double2*)dst);
+        else
+            k_unpack<decltype(L), T, float2><<<nb, 256, 0, st>>>(L, U.g, (float2*)dst);
+    });
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// batched MultiplyMatMat (src/SU3MatrixOps.f90:19-37) / MultiplyMatdagMatdag
+// (:39-58; its code forms conj(sum_k L(k,i) R(j,k)) = (L^+ R^+)(i,j), although
+// its comment reads (L R)^+): n matrices of 9 complex, Fortran order (a + 3b).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_matmul_batch(const typename V2<T>::type* __restrict__ l, const typename V2<T>::type* __restrict__ r,
+                               typename V2<T>::type* __restrict__ o, int64_t n, int dagger) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    M3<T> A, B;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const auto x = l[9 * j + a + 3 * b];
+            const auto y = r[9 * j + a + 3 * b];
+            A.r[3 * a + b] = x.x;
+            A.i[3 * a + b] = x.y;
+            B.r[3 * a + b] = y.x;
+            B.i[3 * a + b] = y.y;
+        }
+    // MultiplyMatdagMatdag computes L^+ R^+ (src/SU3MatrixOps.f90:47-57)
+    const M3<T> C = dagger ? mm<true, true>(A, B) : mul(A, B);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            typename V2<T>::type v;
+            v.x = C.r[3 * a + b];
+            v.y = C.i[3 * a + b];
+            o[9 * j + a + 3 * b] = v;
+        }
+}
+
+cudaError_t launch_matmul_batch(const void* l, const void* r, void* o, int64_t n, int dtype, int dagger, cudaStream_t st) {
+    const unsigned nb = (unsigned)((n + 127) / 128);
+    if (dtype == PREC_C128)
+        k_matmul_batch<double><<<nb, 128, 0, st>>>((const double2*)l, (const double2*)r, (double2*)o, n, dagger);
+    else
+        k_matmul_batch<float><<<nb, 128, 0, st>>>((const float2*)l, (const float2*)r, (float2*)o, n, dagger);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// plaquette over planes mu in [mu0,mu1], nu in (mu,nu1] (0-based):
+// Re Tr[(U_mu(x) U_nu(x+mu)) (U_mu(x+nu) U_nu(x))^+]  (src/wloops.F90:960-1005)
+// ---------------------------------------------------------------------------
+constexpr int RED_BS = 256;
+
+int plaquette_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
+
+template <class L, typename T>
+__global__ void __launch_bounds__(RED_BS) k_plaquette(L U, Geom g, int mu0, int mu1, int nu1, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.V; s += (int64_t)gridDim.x * blockDim.x) {
+        int c[4];
+        site_coords(g, s, c);
+        for (int mu = mu0; mu <= mu1; ++mu) {
+            const int64_t smu = s + disp(g, mu, c[mu], 1);
+            const M3<T> umu = U.load(s, mu);
+            for (int nu = mu + 1; nu <= nu1; ++nu) {
+                const int64_t snu = s + disp(g, nu, c[nu], 1);
+                // MultiplyMatdagMatdag(Umu_xnu, Unu_x) = Umu_xnu^+ Unu_x^+ = (Unu_x Umu_xnu)^+
+                const M3<T> a = mul(umu, U.load(smu, nu));
+                const M3<T> b = mul(U.load(s, nu), U.load(snu, mu));
+                acc += (double)retr_mm<false, true>(a, b);
+            }
+        }
+    }
+    const double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+cudaError_t launch_plaquette(const FieldRef& U, int mu0, int mu1, int nu1, double* part, double* out, cudaStream_t st) {
+    const int nb = plaquette_blocks(U.g);
+    FLUE_DISPATCH_LINKS(U, k_plaquette<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, mu0, mu1, nu1, part));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_finish_sums(part, nb, 1, out, st);
+}
+
+// ---------------------------------------------------------------------------
+// Polyakov loop: ordered product of U_t over t = 1..NT at every spatial site
+// (src/wloops.F90:1043-1066); out2 = [sum Re Tr, sum Im Tr].
+// ---------------------------------------------------------------------------
+int polyakov_blocks(const Geom& g) { return grid_for(g.V / g.n[0], RED_BS, 4 * 152); }
+
+template <class L, typename T>
+__global__ void __launch_bounds__(RED_BS) k_polyakov(L U, Geom g, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double accr = 0.0, acci = 0.0;
+    const int64_t V3 = g.V / g.n[0];
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < V3; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s0 = r * g.n[0];
+        M3<T> p = U.load(s0, 0);
+        for (int t = 1; t < g.n[0]; ++t) p = mul(p, U.load(s0 + t, 0));
+        accr += (double)retr(p);
+        acci += (double)(p.i[0] + p.i[4] + p.i[8]);
+    }
+    double a = block_sum(accr, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+    a = block_sum(acci, sh);
+    if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = a;
+}
+
+cudaError_t launch_polyakov(const FieldRef& U, double* part, double* out2, cudaStream_t st) {
+    const int nb = polyakov_blocks(U.g);
+    FLUE_DISPATCH_LINKS(U, k_polyakov<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, part));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_finish_sums(part, nb, 2, out2, st);
+}
+
+// ---------------------------------------------------------------------------
+// nMu x nNu Wilson loop at every site (tau < 0) or on the slice t = tau
+// (src/wloops.F90:599-675 and :711-789).
+// ---------------------------------------------------------------------------
+int wloop_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
+
+template <class L, typename T>
+__device__ __forceinline__ M3<T> line_walk(const L& U, const Geom& g, int64_t s, const int c[4], int mu, int n) {
+    // product U_mu(x) U_mu(x+mu) ... of n links starting at site s (coords c)
+    M3<T> p = U.load(s, mu);
+    int cm = c[mu];
+    for (int k = 1; k < n; ++k) {
+        const int64_t d = disp(g, mu, cm, 1);
+        s += d;
+        cm = (cm + 1 == g.n[mu]) ? 0 : cm + 1;
+        p = mul(p, U.load(s, mu));
+    }
+    return p;
+}
+
+template <class L, typename T>
+__global__ void __launch_bounds__(RED_BS)
+    k_wloop(L U, Geom g, int tau, int mu, int nu, int nmu, int nnu, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    const int64_t nsites = tau < 0 ? g.V : g.V / g.n[0];
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nsites; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = tau < 0 ? j : (int64_t)tau + j * g.n[0];
+        int c[4];
+        site_coords(g, s, c);
+        const M3<T> a = line_walk<L, T>(U, g, s, c, mu, nmu);
+        int c2[4] = {c[0], c[1], c[2], c[3]};
+        const int64_t dmu = disp(g, mu, c[mu], nmu);
+        c2[mu] = (int)(((int64_t)c[mu] + nmu) % g.n[mu]);
+        const M3<T> b = line_walk<L, T>(U, g, s + dmu, c2, nu, nnu);
+        int c3[4] = {c[0], c[1], c[2], c[3]};
+        const int64_t dnu = disp(g, nu, c[nu], nnu);
+        c3[nu] = (int)(((int64_t)c[nu] + nnu) % g.n[nu]);
+        const M3<T> cc = line_walk<L, T>(U, g, s + dnu, c3, mu, nmu);
+        const M3<T> d = line_walk<L, T>(U, g, s, c, nu, nnu);
+        // Re Tr[(A B) (C^+ D^+)] with C^+ D^+ = (D C)^+  (MultiplyMatdagMatdag, :669)
+        const M3<T> ab = mul(a, b);
+        const M3<T> dc = mul(d, cc);
+        acc += (double)retr_mm<false, true>(ab, dc);
+    }
+    const double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+cudaError_t launch_wloop(const FieldRef& U, int tau, int mu, int nu, int nmu, int nnu, double* part, double* out,
+                         cudaStream_t st) {
+    const int nb = wloop_blocks(U.g);
+    FLUE_DISPATCH_LINKS(U, k_wloop<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, tau, mu, nu, nmu, nnu, part));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const double norm = tau < 0 ? (double)U.g.V : (double)(U.g.V / U.g.n[0]);
+    return launch_finish_sums(part, nb, 1, out, st, 1.0 / norm);
+}
+
+// ---------------------------------------------------------------------------
+// genericPath (src/wloops.F90:20-57) at every site or one site.  Output is the
+// TRANSPOSE of the ordered product, in the layout (NT,NX,NY,NZ,3,3) (or one
+// 3x3 Fortran-ordered matrix), complex128 for FP64 fields, complex64 else.
+// ---------------------------------------------------------------------------
+constexpr int MAX_PATH = 256;
+struct PathArg {
+    int n;
+    int step[MAX_PATH];  // +-(mu+1)
+};
+
+template <class L, typename T>
+__global__ void k_genericpath(L U, Geom g, PathArg path, int64_t s_single, typename V2<T>::type* __restrict__ out) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool single = s_single >= 0;
+    if (single ? j > 0 : j >= g.V) return;
+    const int64_t s0 = single ? s_single : j;
+    int c[4];
+    site_coords(g, s0, c);
+    int64_t s = s0;
+    M3<T> p = m_ident<T>();
+    for (int k = 0; k < path.n; ++k) {
+        const int st = path.step[k];
+        if (st < 0) {
+            const int mu = -st - 1;
+            s += disp(g, mu, c[mu], -1);
+            c[mu] = c[mu] == 0 ? g.n[mu] - 1 : c[mu] - 1;
+            p = mm<false, true>(p, U.load(s, mu));
+        } else {
+            const int mu = st - 1;
+            p = mul(p, U.load(s, mu));
+            s += disp(g, mu, c[mu], 1);
+            c[mu] = (c[mu] + 1 == g.n[mu]) ? 0 : c[mu] + 1;
+        }
+    }
+    RefOut<T> o{out, single ? 1 : g.V, 1};
+    o.store(single ? 0 : s0, 0, transp(p));
+}
+
+cudaError_t launch_genericpath(const FieldRef& U, const int* path_host, int npath, const int* coord_host, void* out,
+                               cudaStream_t st) {
+    PathArg pa;
+    pa.n = npath;
+    for (int k = 0; k < npath; ++k) pa.step[k] = path_host[k];
+    int64_t ss = -1;
+    if (coord_host) {
+        ss = (int64_t)(coord_host[0] - 1) + U.g.st[1] * (coord_host[1] - 1) + U.g.st[2] * (coord_host[2] - 1) +
+             U.g.st[3] * (coord_host[3] - 1);
+    }
+    const unsigned nb = coord_host ? 1u : (unsigned)((U.g.V + 127) / 128);
+    FLUE_DISPATCH_LINKS(U, k_genericpath<decltype(L), T><<<nb, 128, 0, st>>>(L, U.g, pa, ss, (typename V2<T>::type*)out));
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Landau-gauge mean link: per direction sum over sites of
+// Re Tr(G(x) U_mu(x) G(x+mu)^+), G in (NT,NX,NY,NZ,3,3) layout.
+// ---------------------------------------------------------------------------
+int meanlink_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
+
+template <typename T, typename G2>
+__device__ __forceinline__ M3<T> load_g(const G2* __restrict__ G, int64_t V, int64_t s) {
+    M3<T> m;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const G2 v = G[s + V * (a + 3 * b)];
+            m.r[3 * a + b] = (T)v.x;
+            m.i[3 * a + b] = (T)v.y;
+        }
+    return m;
+}
+
+template <class L, typename T, typename G2>
+__global__ void __launch_bounds__(RED_BS) k_meanlink(L U, Geom g, const G2* __restrict__ G, double* __restrict__ part) {
+    __shared__ double sh[32];
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.V; s += (int64_t)gridDim.x * blockDim.x) {
+        int c[4];
+        site_coords(g, s, c);
+        const M3<T> gx = load_g<T>(G, g.V, s);
+#pragma unroll
+        for (int mu = 0; mu < 4; ++mu) {
+            const M3<T> gp = load_g<T>(G, g.V, s + disp(g, mu, c[mu], 1));
+            const M3<T> gu = mul(gx, U.load(s, mu));
+            acc[mu] += (double)retr_mm<false, true>(gu, gp);
+        }
+    }
+#pragma unroll
+    for (int mu = 0; mu < 4; ++mu) {
+        const double r = block_sum(acc[mu], sh);
+        if (threadIdx.x == 0) part[mu * gridDim.x + blockIdx.x] = r;
+    }
+}
+
+cudaError_t launch_meanlink(const FieldRef& U, const void* G, int g_dtype, double* part, double* out4, cudaStream_t st) {
+    const int nb = meanlink_blocks(U.g);
+    FLUE_DISPATCH_LINKS(U, {
+        if (g_dtype == PREC_C128)
+            k_meanlink<decltype(L), T, double2><<<nb, RED_BS, 0, st>>>(L, U.g, (const double2*)G, part);
+        else
+            k_meanlink<decltype(L), T, float2><<<nb, RED_BS, 0, st>>>(L, U.g, (const float2*)G, part);
+    });
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_finish_sums(part, nb, 4, out4, st);
+}
+
+}  // namespace flue

@@ -1,0 +1,99 @@
+"""GPU gradients: against the oracle's brute-force reverse mode and analytic
+staple force (FP64 to 1e-11), against central finite differences along random
+su(3) directions (FP64, h = 1e-4), the Euclidean / Lie form relation, the
+torch.autograd front end, and the FP32 error bound."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from flue_gb300 import forces, generate, gluonCalc as G
+from flue_gb300.field import GaugeField
+from tests import np_flue
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    return t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else t
+
+
+def _lie_pair(g, x):
+    return float(-2.0 * np.einsum("...ij,...ji->...", x, g).real.sum())
+
+
+def _perturb(U, X, h):
+    return np.asfortranarray(np_flue.expm_su3(h * X) @ U)
+
+
+@pytest.mark.parametrize("dims,eps,seed", [((4, 4, 4, 4), 0.4, 1), ((5, 3, 4, 3), 0.7, 2)])
+def test_magnetic_force_vs_oracle(dims, eps, seed):
+    U = generate.random_field(dims, eps, seed)
+    b, g = forces.magnetic_force(U)
+    assert abs(b - oracle.magnetic(U)) < 1e-12 * max(1, abs(b))
+    go = oracle.loop5_energy_force(U, oracle.B2_PLANES)
+    assert np.abs(_np(g) - go).max() < 1e-11 * max(1.0, np.abs(go).max())
+    assert np.abs(_np(g)[..., 0, :, :]).max() == 0.0
+
+
+def test_energy_force_all_planes_vs_oracle():
+    U = generate.random_field((4, 3, 4, 5), 0.5, 3)
+    e, g = forces.loop5_energy_force(U, forces.ALL_PLANES)
+    assert abs(e - oracle.loop5_energy(U, oracle.ALL_PLANES)) < 1e-12 * abs(e)
+    go = oracle.loop5_energy_force(U, oracle.ALL_PLANES)
+    assert np.abs(_np(g) - go).max() < 1e-11 * np.abs(go).max()
+    # plane orientation does not change the energy
+    e2, g2 = forces.loop5_energy_force(U, ((2, 1), (3, 1), (4, 1), (3, 2), (4, 2), (4, 3)))
+    assert abs(e2 - e) < 1e-12 * abs(e)
+    assert np.abs(_np(g2) - _np(g)).max() < 1e-12
+
+
+def test_plaquette_force_vs_staple():
+    U = generate.random_field((4, 4, 3, 5), 0.6, 4)
+    s, g = forces.plaquette_force(U)
+    assert abs(s - oracle.plaquette(U, 1, 4, 4)[0]) < 1e-12 * abs(s)
+    assert np.abs(_np(g) - oracle.plaquette_staple_force(U)).max() < 1e-12
+
+
+def test_fd_along_random_directions_fp64():
+    U = generate.random_field((8, 6, 6, 6), 0.3, 5)
+    _, g = forces.magnetic_force(U)
+    gn = _np(g)
+    h = 1e-4
+    worst = 0.0
+    for k in range(8):
+        X = generate.random_su3_algebra(U.shape[:5], 100 + k)
+        fd = (G.magnetic(_perturb(U, X, h)) - G.magnetic(_perturb(U, X, -h))) / (2 * h)
+        an = _lie_pair(gn, X)
+        worst = max(worst, abs(an - fd) / abs(fd))
+    assert worst < 1e-6
+
+
+def test_euclid_form_and_autograd():
+    U = generate.random_field((4, 4, 4, 4), 0.5, 6)
+    _, gl = forces.magnetic_force(U, form="lie")
+    _, ge = forces.magnetic_force(U, form="euclid")
+    # Lie gradient from the Euclidean one: G = -1/2 TA(U N), N = Gamma^+
+    m = U @ np_flue.dag(_np(ge))
+    ah = 0.5 * (m - np_flue.dag(m))
+    ta = ah - np.trace(ah, axis1=-2, axis2=-1)[..., None, None] * np.eye(3) / 3
+    assert np.abs(-0.5 * ta - _np(gl)).max() < 1e-13
+    # torch.autograd: directional derivative along a random complex direction
+    Ut = torch.tensor(U, device="cuda", requires_grad=True)
+    b = forces.magnetic_autograd(Ut)
+    b.backward()
+    D = np.random.default_rng(0).standard_normal(U.shape) * (1 + 1j)
+    h = 1e-6
+    fd = (G.magnetic(np.asfortranarray(U + h * D)) - G.magnetic(np.asfortranarray(U - h * D))) / (2 * h)
+    an = float(np.sum((np.conj(_np(Ut.grad)) * D).real))
+    assert abs(an - fd) < 1e-6 * abs(fd)
+
+
+@pytest.mark.parametrize("prec", ["c64", "r12"])
+def test_fp32_force_error_bound(prec):
+    U = generate.random_field((8, 8, 8, 8), 0.3, 7)
+    b64, g64 = forces.magnetic_force(U)
+    b32, g32 = forces.magnetic_force(GaugeField.from_array(U, prec=prec))
+    g64, g32 = _np(g64), _np(g32).astype(np.complex128)
+    assert abs(b32 - b64) / abs(b64) < 1e-6
+    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-5
