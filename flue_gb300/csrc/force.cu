@@ -400,7 +400,7 @@ static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, in
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (out_E) {
-        e = launch_finish_sums(part, (int)(nbx * pa.np), 1, out_E, st);
+        e = launch_finish_sums(part, (int)(nbx * pa.np), 1, out_E, st, 1.0 / (double)g.V);
         if (e != cudaSuccess) return e;
     }
     stage_mark(2, st);

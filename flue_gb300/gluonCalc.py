@@ -340,10 +340,11 @@ def uzerobar(data, G=None, prec=None):
                       _lib.C128 if gd.dtype == torch.complex128 else _lib.C64, _ptr(out[3:7]), _ptr(ws2),
                       ws2.numel(), _stream_handle())
     s = _scalars(out)
-    p_all, p_s, p_t = s[0] / (6 * V) / 3, s[1] / (3 * V) / 3, s[2] / (3 * V) / 3
-    res[0] = p_all ** 0.25
-    res[1] = p_s ** 0.25
-    res[2] = p_t ** 0.5 / res[1]
+    p = np.array([s[0] / (6 * V) / 3, s[1] / (3 * V) / 3, s[2] / (3 * V) / 3])
+    with np.errstate(invalid="ignore"):  # a negative mean plaquette has no real root: NaN
+        res[0] = np.power(p[0], 0.25)
+        res[1] = np.power(p[1], 0.25)
+        res[2] = np.sqrt(p[2]) / res[1]
     if G is not None:
         res[3] = (s[3] + s[4] + s[5] + s[6]) / (4 * V) / 3
         res[4] = (s[4] + s[5] + s[6]) / (3 * V) / 3

@@ -62,7 +62,7 @@ def test_genericpath_fp64(U):
         a = G.genericpath_all(U, path)
         b = oracle.genericpath_all(U, path)
         assert np.abs(a - b).max() < 1e-12
-        cb = [1 + i % U.shape[i] for i in (1, 2, 0, 3)]
+        cb = [1 + (k + 1) % U.shape[k] for k in range(4)]
         g = G.genericpath(U, cb, path)
         assert np.abs(g - oracle.genericpath(U, cb, path)).max() < 1e-12
 
@@ -96,7 +96,10 @@ def test_uzerobar_fp64(U):
     g = generate.random_gauge_transform(U.shape[:4], 8)
     a = G.uzerobar(U, g)
     b = oracle.uzerobar(U, g)
-    assert np.abs(a - b).max() < 1e-12
+    # Haar fields can have <Re Tr P> < 0: both sides give NaN there
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    ok = ~np.isnan(b)
+    assert np.abs(a[ok] - b[ok]).max() < 1e-12
 
 
 def test_su3_helpers():
@@ -132,7 +135,7 @@ def test_cold_field_exact():
     U = generate.cold_field((4, 4, 4, 8))
     V = 4 * 4 * 4 * 8
     assert G.plaquette(U, 1, 4, 4)[:2] == (18.0 * V, 6 * V)
-    assert G.polyakov(U)[:2] == (3.0 * 64, 64)
+    assert G.polyakov(U)[:2] == (3.0 * 128, 128)
     assert G.magnetic(U) == 0.0
 
 
