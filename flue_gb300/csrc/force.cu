@@ -76,6 +76,17 @@ struct PlaneArg {
     int dir[4];   // slot -> direction
 };
 
+// Reads of PlaneArg with a runtime index, written as unrolled selects so that
+// the kernel-parameter struct is never copied to local memory.
+template <int N>
+__device__ __forceinline__ int sel(const int (&a)[N], int i) {
+    int r = a[0];
+#pragma unroll
+    for (int k = 1; k < N; ++k)
+        if (k == i) r = a[k];
+    return r;
+}
+
 // periodic displacement by k along mu from coordinate cmu (any k)
 __device__ __forceinline__ int64_t dsp(const Geom& g, int mu, int cmu, int k) {
     const int n = g.n[mu];
@@ -85,35 +96,65 @@ __device__ __forceinline__ int64_t dsp(const Geom& g, int mu, int cmu, int k) {
     return (int64_t)(t - cmu) * g.st[mu];
 }
 
-template <class L, typename T>
+__device__ __forceinline__ int wrapd(int c, int k, int n) {
+    int t = c + k;
+    while (t < 0) t += n;
+    while (t >= n) t -= n;
+    return t - c;
+}
+
+// Per-thread view of one plane (mu,nu) around the thread's site: every
+// coordinate the stencil needs is kept in scalars (no runtime-indexed
+// arrays, so nothing lands in local memory).
+template <typename T>
 struct Ctx {
-    L U;
-    MatPlanes<T> lines;  // 2 per slot: L^2, L^3
-    Geom g;
+    MatPlanes<T> lines;  // 3 per slot: L^1 (U expanded), L^2, L^3
     int64_t s;
-    int c[4];
-    int mu, nu, smu, snu;  // plane directions and their slots
+    int cm, cn, nm, nn;  // coordinates and extents along mu, nu
+    int64_t stm, stn;    // site strides along mu, nu
+    int kmu, knu;        // first line plane of the mu / nu slot (3 * slot)
     __device__ __forceinline__ int64_t at(int i, int j) const {
-        return s + dsp(g, mu, c[mu], i) + dsp(g, nu, c[nu], j);
-    }
-    __device__ __forceinline__ M3<T> line(int dir, int slot, int len, int64_t site) const {
-        if (len == 1) return U.load(site, dir);
-        return lines.load(site, 2 * slot + len - 2);
+        return s + (int64_t)wrapd(cm, i, nm) * stm + (int64_t)wrapd(cn, j, nn) * stn;
     }
     // side k (1..4) of the rectangle anchored at (i0,j0) with shape (a,b)
     __device__ __forceinline__ M3<T> side(int k, int i0, int j0, int a, int b) const {
         switch (k) {
             case 1:
-                return line(mu, smu, a, at(i0, j0));
+                return lines.load(at(i0, j0), kmu + a - 1);
             case 2:
-                return line(nu, snu, b, at(i0 + a, j0));
+                return lines.load(at(i0 + a, j0), knu + b - 1);
             case 3:
-                return dag(line(mu, smu, a, at(i0, j0 + b)));
+                return dag(lines.load(at(i0, j0 + b), kmu + a - 1));
             default:
-                return dag(line(nu, snu, b, at(i0, j0)));
+                return dag(lines.load(at(i0, j0), knu + b - 1));
         }
     }
 };
+
+template <typename T>
+__device__ __forceinline__ Ctx<T> make_ctx(const MatPlanes<T>& lines, const Geom& g, int64_t s, const int c[4], int mu,
+                                           int nu, int smu, int snu) {
+    Ctx<T> cx;
+    cx.lines = lines;
+    cx.s = s;
+    // select without runtime indexing of c[] / g.n[] / g.st[]
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        if (d == mu) {
+            cx.cm = c[d];
+            cx.nm = g.n[d];
+            cx.stm = g.st[d];
+        }
+        if (d == nu) {
+            cx.cn = c[d];
+            cx.nn = g.n[d];
+            cx.stn = g.st[d];
+        }
+    }
+    cx.kmu = 3 * smu;
+    cx.knu = 3 * snu;
+    return cx;
+}
 
 __device__ __forceinline__ void corner_off(int k, int a, int b, int& di, int& dj) {
     di = (k == 2 || k == 3) ? a : 0;
@@ -121,21 +162,29 @@ __device__ __forceinline__ void corner_off(int k, int a, int b, int& di, int& dj
 }
 
 // ---------------------------------------------------------------------------
-// 1. lines: L^2_d(y) = U_d(y) U_d(y+d), L^3_d(y) = L^2_d(y) U_d(y+2d)
+// 1. lines: L^1_d(y) = U_d(y) (expanded to 18 reals), L^2_d(y) = U_d(y) U_d(y+d),
+//    L^3_d(y) = L^2_d(y) U_d(y+2d)
 // ---------------------------------------------------------------------------
 template <class L, typename T>
 __global__ void k_lines(L U, Geom g, PlaneArg pa, MatPlanes<T> lines) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     const int slot = blockIdx.y;
-    const int d = pa.dir[slot];
+    const int d = sel(pa.dir, slot);
     int c[4];
     site_coords(g, s, c);
-    const int64_t s1 = s + dsp(g, d, c[d], 1);
-    const int64_t s2 = s + dsp(g, d, c[d], 2);
-    const M3<T> l2 = mul(U.load(s, d), U.load(s1, d));
-    lines.store(s, 2 * slot, l2);
-    lines.store(s, 2 * slot + 1, mul(l2, U.load(s2, d)));
+    int cd = 0, nd = 1;
+    int64_t sd = 1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
+    const int64_t s1 = s + (int64_t)wrapd(cd, 1, nd) * sd;
+    const int64_t s2 = s + (int64_t)wrapd(cd, 2, nd) * sd;
+    const M3<T> u0 = U.load(s, d);
+    const M3<T> l2 = mul(u0, U.load(s1, d));
+    lines.store(s, 3 * slot, u0);
+    lines.store(s, 3 * slot + 1, l2);
+    lines.store(s, 3 * slot + 2, mul(l2, U.load(s2, d)));
 }
 
 // ---------------------------------------------------------------------------
@@ -143,16 +192,19 @@ __global__ void k_lines(L U, Geom g, PlaneArg pa, MatPlanes<T> lines) {
 // ---------------------------------------------------------------------------
 constexpr int FWD_BS = 128;
 
-template <class L, typename T>
+template <typename T>
 __global__ void __launch_bounds__(FWD_BS)
-    k_fwd(L U, Geom g, PlaneArg pa, int kind, MatPlanes<T> lines, AHPlanes<T> kout, RefOut<T> fout, double* part) {
+    k_fwd(Geom g, PlaneArg pa, int kind, MatPlanes<T> lines, AHPlanes<T> kout, RefOut<T> fout, double* part) {
     __shared__ double sh[32];
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int p = blockIdx.y;
+    // planes of the same site block run in adjacent blocks (L2 reuse)
+    const int p = blockIdx.x % pa.np;
+    const int64_t s = (int64_t)(blockIdx.x / pa.np) * blockDim.x + threadIdx.x;
     double e = 0.0;
     if (s < g.V) {
-        Ctx<L, T> cx{U, lines, g, s, {0, 0, 0, 0}, pa.mu[p], pa.nu[p], pa.slot[pa.mu[p]], pa.slot[pa.nu[p]]};
-        site_coords(g, s, cx.c);
+        int c[4];
+        site_coords(g, s, c);
+        const int pmu = sel(pa.mu, p), pnu = sel(pa.nu, p);
+        const Ctx<T> cx = make_ctx(lines, g, s, c, pmu, pnu, sel(pa.slot, pmu), sel(pa.slot, pnu));
         const Shape* shp = kind == 1 ? c_shapes5 : c_shapes1;
         const int nsh = kind == 1 ? 7 : 1;
         M3<T> q = m_zero<T>();
@@ -180,7 +232,7 @@ __global__ void __launch_bounds__(FWD_BS)
     }
     if (part) {
         const double r = block_sum(e, sh);
-        if (threadIdx.x == 0) part[(int64_t)p * gridDim.x + blockIdx.x] = r;
+        if (threadIdx.x == 0) part[blockIdx.x] = r;
     }
 }
 
@@ -189,8 +241,8 @@ __global__ void __launch_bounds__(FWD_BS)
 // ---------------------------------------------------------------------------
 constexpr int COT_BS = 128;
 
-template <class L, typename T>
-__device__ __forceinline__ M3<T> corner_k(const Ctx<L, T>& cx, const AHPlanes<T>& kin, int p, int k, int i0, int j0, int a,
+template <typename T>
+__device__ __forceinline__ M3<T> corner_k(const Ctx<T>& cx, const AHPlanes<T>& kin, int p, int k, int i0, int j0, int a,
                                           int b) {
     int di, dj;
     corner_off(k, a, b, di, dj);
@@ -200,8 +252,8 @@ __device__ __forceinline__ M3<T> corner_k(const Ctx<L, T>& cx, const AHPlanes<T>
 // Sum of the four corner insertions in the word that follows side q of the
 // rectangle (i0,j0,a,b):  Ka A B C + A Kb B C + A B Kc C + A B C Kd with
 // A,B,C = S_q+1, S_q+2, S_q+3 and Ka,Kb,Kc,Kd = K_q+1, K_q+2, K_q+3, K_q.
-template <class L, typename T>
-__device__ __forceinline__ M3<T> side_cot(const Ctx<L, T>& cx, const AHPlanes<T>& kin, int p, int q, int i0, int j0, int a,
+template <typename T>
+__device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHPlanes<T>& kin, int p, int q, int i0, int j0, int a,
                                           int b) {
     const int q1 = q % 4 + 1, q2 = q1 % 4 + 1, q3 = q2 % 4 + 1;
     const M3<T> C = cx.side(q3, i0, j0, a, b);
@@ -229,21 +281,26 @@ __device__ __forceinline__ M3<T> side_cot(const Ctx<L, T>& cx, const AHPlanes<T>
     return res;
 }
 
-template <class L, typename T>
+template <typename T>
 __global__ void __launch_bounds__(COT_BS)
-    k_linecot(L U, Geom g, PlaneArg pa, MatPlanes<T> lines, AHPlanes<T> kin, MatPlanes<T> lam) {
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    k_linecot(Geom g, PlaneArg pa, MatPlanes<T> lines, AHPlanes<T> kin, MatPlanes<T> lam) {
+    // the 3 * nd (direction, length) tasks of one site block run in adjacent
+    // blocks, so the neighbourhood they all read stays in L2
+    const int ntask = 3 * pa.nd;
+    const int task = blockIdx.x % ntask;
+    const int64_t s = (int64_t)(blockIdx.x / ntask) * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
-    const int slot = blockIdx.y / 3;
-    const int len = blockIdx.y % 3 + 1;
-    const int d = pa.dir[slot];
+    const int slot = task / 3;
+    const int len = task % 3 + 1;
+    const int d = sel(pa.dir, slot);
     int c[4];
     site_coords(g, s, c);
     M3<T> acc = m_zero<T>();
     for (int p = 0; p < pa.np; ++p) {
-        const bool is_mu = pa.mu[p] == d, is_nu = pa.nu[p] == d;
+        const bool is_mu = sel(pa.mu, p) == d, is_nu = sel(pa.nu, p) == d;
         if (!is_mu && !is_nu) continue;
-        Ctx<L, T> cx{U, lines, g, s, {c[0], c[1], c[2], c[3]}, pa.mu[p], pa.nu[p], pa.slot[pa.mu[p]], pa.slot[pa.nu[p]]};
+        const int pmu = sel(pa.mu, p), pnu = sel(pa.nu, p);
+        const Ctx<T> cx = make_ctx(lines, g, s, c, pmu, pnu, sel(pa.slot, pmu), sel(pa.slot, pnu));
         for (int k = 0; k < 7; ++k) {
             const int a = c_shapes5[k].a, b = c_shapes5[k].b;
             const T coef = (T)c_shapes5[k].c;
@@ -267,33 +324,39 @@ __global__ void __launch_bounds__(COT_BS)
 // ---------------------------------------------------------------------------
 // 4. link cotangents and gradient output: one thread per (site, direction)
 // ---------------------------------------------------------------------------
-template <class L, typename T>
-__global__ void k_linkcot(L U, Geom g, PlaneArg pa, MatPlanes<T> lines, MatPlanes<T> lam, T scale, int form,
-                          RefOut<T> out) {
+template <typename T>
+__global__ void k_linkcot(Geom g, PlaneArg pa, MatPlanes<T> lines, MatPlanes<T> lam, T scale, int form, RefOut<T> out) {
     const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (z >= g.V) return;
     const int d = blockIdx.y;
-    const int slot = pa.slot[d];
+    const int slot = sel(pa.slot, d);
     if (slot < 0) {
         out.store(z, d, m_zero<T>());
         return;
     }
     int c[4];
     site_coords(g, z, c);
-    const int64_t zp = z + dsp(g, d, c[d], 1), zm = z + dsp(g, d, c[d], -1), zmm = z + dsp(g, d, c[d], -2);
-    const M3<T> up = U.load(zp, d);
-    const M3<T> um = U.load(zm, d);
+    int cd = 0, nd = 1;
+    int64_t sd = 1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
+    const int64_t zp = z + (int64_t)wrapd(cd, 1, nd) * sd, zm = z + (int64_t)wrapd(cd, -1, nd) * sd,
+                  zmm = z + (int64_t)wrapd(cd, -2, nd) * sd;
+    const int l1 = 3 * slot, l2 = 3 * slot + 1;
+    const M3<T> up = lines.load(zp, l1);
+    const M3<T> um = lines.load(zm, l1);
     M3<T> n = lam.load(z, 3 * slot);
     mac<false, false>(n, up, lam.load(z, 3 * slot + 1));
     mac<false, false>(n, lam.load(zm, 3 * slot + 1), um);
-    mac<false, false>(n, lines.load(zp, 2 * slot), lam.load(z, 3 * slot + 2));
+    mac<false, false>(n, lines.load(zp, l2), lam.load(z, 3 * slot + 2));
     {
         const M3<T> t = mul(up, lam.load(zm, 3 * slot + 2));
         mac<false, false>(n, t, um);
     }
-    mac<false, false>(n, lam.load(zmm, 3 * slot + 2), lines.load(zmm, 2 * slot));
+    mac<false, false>(n, lam.load(zmm, 3 * slot + 2), lines.load(zmm, l2));
     if (form == 0) {
-        const M3<T> un = mul(U.load(z, d), n);
+        const M3<T> un = mul(lines.load(z, l1), n);
         out.store(z, d, ta_scaled(un, T(-0.5) * scale));
     } else {
         out.store(z, d, m_scale(dag(n), scale));
@@ -332,7 +395,7 @@ static EnergyWs energy_layout(const Geom& g, int prec, const PlaneArg& pa, bool 
     EnergyWs w;
     const int nbx = (int)((g.V + FWD_BS - 1) / FWD_BS);
     w.lines = 0;
-    w.kbuf = align256(w.lines + (size_t)2 * pa.nd * 9 * g.V * 2 * cs);
+    w.kbuf = align256(w.lines + (size_t)3 * pa.nd * 9 * g.V * 2 * cs);
     w.lam = align256(w.kbuf + (with_force ? (size_t)pa.np * 9 * g.V * cs : 0));
     w.part = align256(w.lam + (with_force ? (size_t)3 * pa.nd * 9 * g.V * 2 * cs : 0));
     w.total = align256(w.part + (size_t)pa.np * nbx * sizeof(double));
@@ -396,7 +459,7 @@ static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, in
     stage_mark(0, st);
     k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, pa, lines);
     stage_mark(1, st);
-    k_fwd<L, T><<<dim3(nbx, pa.np), FWD_BS, 0, st>>>(U, g, pa, kind, lines, kb, fout, part);
+    k_fwd<T><<<nbx * pa.np, FWD_BS, 0, st>>>(g, pa, kind, lines, kb, fout, part);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (out_E) {
@@ -406,11 +469,11 @@ static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, in
     stage_mark(2, st);
     if (!force) return cudaSuccess;
     const unsigned nbc = (unsigned)((g.V + COT_BS - 1) / COT_BS);
-    k_linecot<L, T><<<dim3(nbc, 3 * pa.nd), COT_BS, 0, st>>>(U, g, pa, lines, kb, lam);
+    k_linecot<T><<<nbc * 3 * pa.nd, COT_BS, 0, st>>>(g, pa, lines, kb, lam);
     stage_mark(3, st);
     RefOut<T> fo{(C2*)force, g.V, 4};
     const T scale = (T)(-1.0 / (2.0 * (double)g.V));
-    k_linkcot<L, T><<<dim3((unsigned)((g.V + 127) / 128), 4), 128, 0, st>>>(U, g, pa, lines, lam, scale, form, fo);
+    k_linkcot<T><<<dim3((unsigned)((g.V + 127) / 128), 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo);
     stage_mark(4, st);
     return cudaGetLastError();
 }
