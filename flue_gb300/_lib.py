@@ -77,6 +77,7 @@ SIGNATURES = {
     "flue_reunitarise_field": ([_FP, _P], _I),
     "flue_multiplymatmat_batch": ([_P, _P, _P, _I64, _I, _I, _P], _I),
     "flue_plaquette": ([_FP, _I, _I, _I, _P, _P, _SZ, _P], _I),
+    "flue_plaquette_noalloc": ([_FP, _I, _I, _I, _P, _P], _I),
     "flue_polyakov": ([_FP, _P, _P, _SZ, _P], _I),
     "flue_wmunu": ([_FP, _I, _I, _I, _I, _I, _P, _P, _SZ, _P], _I),
     "flue_genericpath": ([_FP, _P, _P, _I, _P, _P], _I),

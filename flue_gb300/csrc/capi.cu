@@ -131,6 +131,8 @@ int energy_common(const flue_field* U, const PlaneSet& ps, int op, double* d_E, 
 
 }  // namespace
 
+void flue::set_error_detail(const char* msg) { snprintf(g_detail, sizeof(g_detail), "%s", msg); }
+
 extern "C" {
 
 const char* flue_strerror(int s) {

@@ -54,6 +54,9 @@ int plaqforce_blocks(const Geom& g);
 cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_S, void* force, int force_form,
                                    cudaStream_t st);
 
+// text returned by flue_last_error_detail() on the calling thread
+void set_error_detail(const char* msg);
+
 cudaError_t stage_timing_enable(int on);
 cudaError_t stage_times(double* ms, int maxn, int* n);
 

@@ -181,6 +181,21 @@ int flue_meanlink(const flue_field *U, const void *G, int g_dtype, double *d_sum
  * field must be FLUE_C128 or FLUE_C64. */
 int flue_wflow_step(const flue_field *U, double eps, void *ws, size_t ws_bytes, void *stream);
 
+/* Allocation-free plaquette.  No counterpart in the reference.  Same result
+ * as flue_plaquette (same kernel, bitwise the same sum) but without a
+ * workspace argument: the per-block partial sums live in an 8 KiB array that
+ * is part of the library's device image, so the call allocates nothing --
+ * for callers that own all device memory themselves (a simulation measuring
+ * the plaquette in its update loop through ISO_C_BINDING while its pool holds
+ * the HBM, or a framework whose allocator this library cannot reach).  Limit:
+ * 1024 partial sums; the plaquette launch never uses more than 608 blocks, so
+ * every lattice the ABI accepts fits, and a larger need is refused with
+ * FLUE_ERR_WORKSPACE.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int flue_plaquette_noalloc(const flue_field *U, int muStart, int muEnd, int nuEnd, double *d_sum, void *stream);
+
 /* ======================================================================== */
 /* Tier 1: host-buffer entry points (reference signatures)                  */
 /* data: host complex128 (NT,NX,NY,NZ,4,3,3), Fortran order.                */
