@@ -47,15 +47,21 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, extra_flags=(), lib_path: str | None = None,
+          build_dir: str | None = None) -> str:
+    """Compile and link the library.  ``extra_flags`` / ``lib_path`` /
+    ``build_dir`` build a separately named copy (e.g. with different tuning
+    macros) without touching the default library."""
+    lib = lib_path or LIB
+    bdir = build_dir or BUILD
+    if not force and lib == LIB and not extra_flags and up_to_date():
         return LIB
-    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(bdir, exist_ok=True)
     cc = nvcc()
     srcs = _sources()
 
     def compile_one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(bdir, os.path.basename(src)[:-3] + ".o")
         cmd = [cc, *ARCH, *NVFLAGS, *extra_flags, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -66,13 +72,13 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + f".tmp{os.getpid()}"
+    tmp = lib + f".tmp{os.getpid()}"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -116,18 +116,16 @@ struct Ctx {
     __device__ __forceinline__ int64_t at(int i, int j) const {
         return s + (int64_t)wrapd(cm, i, nm) * stm + (int64_t)wrapd(cn, j, nn) * stn;
     }
-    // side k (1..4) of the rectangle anchored at (i0,j0) with shape (a,b)
+    // side k (1..4) of the rectangle anchored at (i0,j0) with shape (a,b):
+    // S1 = L^a_mu(i0,j0), S2 = L^b_nu(i0+a,j0), S3 = L^a_mu(i0,j0+b)^+,
+    // S4 = L^b_nu(i0,j0)^+.  Selected arithmetically (one load site in the
+    // code for any k) to keep the kernels' instruction footprint small.
     __device__ __forceinline__ M3<T> side(int k, int i0, int j0, int a, int b) const {
-        switch (k) {
-            case 1:
-                return lines.load(at(i0, j0), kmu + a - 1);
-            case 2:
-                return lines.load(at(i0 + a, j0), knu + b - 1);
-            case 3:
-                return dag(lines.load(at(i0, j0 + b), kmu + a - 1));
-            default:
-                return dag(lines.load(at(i0, j0), knu + b - 1));
-        }
+        const bool isnu = (k & 1) == 0;
+        const int plane = isnu ? knu + b - 1 : kmu + a - 1;
+        const int i = i0 + (k == 2 ? a : 0), j = j0 + (k == 3 ? b : 0);
+        const M3<T> m = lines.load(at(i, j), plane);
+        return k >= 3 ? dag(m) : m;
     }
 };
 
@@ -190,10 +188,24 @@ __global__ void k_lines(L U, Geom g, PlaneArg pa, MatPlanes<T> lines) {
 // ---------------------------------------------------------------------------
 // 2. forward: one thread per (site, plane)
 // ---------------------------------------------------------------------------
-constexpr int FWD_BS = 128;
+// block size and minimum resident blocks per SM (register budget) of the
+// forward and line-cotangent kernels; overridable at build time
+#ifndef FLUE_FWD_BS
+#define FLUE_FWD_BS 128
+#endif
+#ifndef FLUE_FWD_MINB
+#define FLUE_FWD_MINB 1
+#endif
+#ifndef FLUE_COT_BS
+#define FLUE_COT_BS 128
+#endif
+#ifndef FLUE_COT_MINB
+#define FLUE_COT_MINB 1
+#endif
+constexpr int FWD_BS = FLUE_FWD_BS;
 
 template <typename T>
-__global__ void __launch_bounds__(FWD_BS)
+__global__ void __launch_bounds__(FWD_BS, FLUE_FWD_MINB)
     k_fwd(Geom g, PlaneArg pa, int kind, MatPlanes<T> lines, AHPlanes<T> kout, RefOut<T> fout, double* part) {
     __shared__ double sh[32];
     // planes of the same site block run in adjacent blocks (L2 reuse)
@@ -208,21 +220,21 @@ __global__ void __launch_bounds__(FWD_BS)
         const Shape* shp = kind == 1 ? c_shapes5 : c_shapes1;
         const int nsh = kind == 1 ? 7 : 1;
         M3<T> q = m_zero<T>();
-        for (int k = 0; k < nsh; ++k) {
+        // one loop over the 4 * nsh leaves, a single copy of the leaf body
+#pragma unroll 1
+        for (int lf = 0; lf < 4 * nsh; ++lf) {
+            const int k = lf >> 2, qd = (lf & 3) + 1;
             const int a = shp[k].a, b = shp[k].b;
-            M3<T> w = m_zero<T>();
-            for (int qd = 1; qd <= 4; ++qd) {
-                int di, dj;
-                corner_off(qd, a, b, di, dj);
-                const int i0 = -di, j0 = -dj;
-                const M3<T> s0 = cx.side(qd, i0, j0, a, b);
-                const M3<T> s1 = cx.side(qd % 4 + 1, i0, j0, a, b);
-                const M3<T> t01 = mul(s0, s1);
-                const M3<T> s2 = cx.side((qd + 1) % 4 + 1, i0, j0, a, b);
-                const M3<T> t012 = mul(t01, s2);
-                const M3<T> s3 = cx.side((qd + 2) % 4 + 1, i0, j0, a, b);
-                mac<false, false>(w, t012, s3);
-            }
+            int di, dj;
+            corner_off(qd, a, b, di, dj);
+            const int i0 = -di, j0 = -dj;
+            const M3<T> s0 = cx.side(qd, i0, j0, a, b);
+            const M3<T> s1 = cx.side(qd % 4 + 1, i0, j0, a, b);
+            const M3<T> t01 = mul(s0, s1);
+            const M3<T> s2 = cx.side((qd + 1) % 4 + 1, i0, j0, a, b);
+            const M3<T> t012 = mul(t01, s2);
+            const M3<T> s3 = cx.side((qd + 2) % 4 + 1, i0, j0, a, b);
+            M3<T> w = mul(t012, s3);
             m_axpy(q, (T)shp[k].c, w);
         }
         const M3<T> f = ah_quarter(q);
@@ -239,7 +251,7 @@ __global__ void __launch_bounds__(FWD_BS)
 // ---------------------------------------------------------------------------
 // 3. line cotangents: one thread per (site, slot, length)
 // ---------------------------------------------------------------------------
-constexpr int COT_BS = 128;
+constexpr int COT_BS = FLUE_COT_BS;
 
 template <typename T>
 __device__ __forceinline__ M3<T> corner_k(const Ctx<T>& cx, const AHPlanes<T>& kin, int p, int k, int i0, int j0, int a,
@@ -282,7 +294,7 @@ __device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHPlanes<T>& k
 }
 
 template <typename T>
-__global__ void __launch_bounds__(COT_BS)
+__global__ void __launch_bounds__(COT_BS, FLUE_COT_MINB)
     k_linecot(Geom g, PlaneArg pa, MatPlanes<T> lines, AHPlanes<T> kin, MatPlanes<T> lam) {
     // the 3 * nd (direction, length) tasks of one site block run in adjacent
     // blocks, so the neighbourhood they all read stays in L2
@@ -297,25 +309,28 @@ __global__ void __launch_bounds__(COT_BS)
     site_coords(g, s, c);
     M3<T> acc = m_zero<T>();
     for (int p = 0; p < pa.np; ++p) {
-        const bool is_mu = sel(pa.mu, p) == d, is_nu = sel(pa.nu, p) == d;
-        if (!is_mu && !is_nu) continue;
         const int pmu = sel(pa.mu, p), pnu = sel(pa.nu, p);
+        const bool is_mu = pmu == d, is_nu = pnu == d;
+        if (!is_mu && !is_nu) continue;
         const Ctx<T> cx = make_ctx(lines, g, s, c, pmu, pnu, sel(pa.slot, pmu), sel(pa.slot, pnu));
-        for (int k = 0; k < 7; ++k) {
+        // A mu-line of length len is side S1 of the rectangle anchored at the
+        // site and S3 (daggered) of the one anchored b below, for every shape
+        // (len, b); a nu-line is S2 of the rectangle anchored a to the left
+        // and S4 (daggered) of the one anchored at the site, for every shape
+        // (a, len).  One loop, one copy of the 8-product body.
+#pragma unroll 1
+        for (int t = 0; t < 14; ++t) {
+            const int k = t >> 1, second = t & 1;
             const int a = c_shapes5[k].a, b = c_shapes5[k].b;
+            if ((is_mu ? a : b) != len) continue;
+            const int q = is_mu ? (second ? 3 : 1) : (second ? 4 : 2);
+            const int i0 = (q == 2) ? -a : 0, j0 = (q == 3) ? -b : 0;
+            const M3<T> r = side_cot(cx, kin, p, q, i0, j0, a, b);
             const T coef = (T)c_shapes5[k].c;
-            if (is_mu && a == len) {
-                // the line is S1 of the rectangle anchored here ...
-                m_axpy(acc, coef, side_cot(cx, kin, p, 1, 0, 0, a, b));
-                // ... and S3 (daggered) of the one anchored b below.
-                m_axpy_dag(acc, coef, side_cot(cx, kin, p, 3, 0, -b, a, b));
-            }
-            if (is_nu && b == len) {
-                // S2 of the rectangle anchored a to the left ...
-                m_axpy(acc, coef, side_cot(cx, kin, p, 2, -a, 0, a, b));
-                // ... and S4 (daggered) of the one anchored here.
-                m_axpy_dag(acc, coef, side_cot(cx, kin, p, 4, 0, 0, a, b));
-            }
+            if (second)
+                m_axpy_dag(acc, coef, r);
+            else
+                m_axpy(acc, coef, r);
         }
     }
     lam.store(s, 3 * slot + len - 1, acc);
