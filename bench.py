@@ -59,7 +59,50 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--ensemble", action="store_true",
+                   help="also time the 96-field ensemble (plaquette/Polyakov/B^2 in one graph-captured launch)")
     return p.parse_args()
+
+
+def ensemble_bench(steps: int):
+    """96 fields: L in {16,24,32} x T in {32,48,64}, 8 each, plus 24 at 24^3x48,
+    eps = 0.4, per-field seeds (GPU Philox); FP32 (c64) and FP64 (c128)."""
+    import torch
+
+    from flue_gb300 import ensemble as E, generate
+    from flue_gb300.field import GaugeField
+
+    dims = [(t, l, l, l) for l in (16, 24, 32) for t in (32, 48, 64) for _ in range(8)] + [(48, 24, 24, 24)] * 24
+    sites = sum(d[0] * d[1] ** 3 for d in dims)
+    t0 = time.perf_counter()
+    f64 = [generate.random_field_philox(d, 0.4, 5000 + i, prec="c128") for i, d in enumerate(dims)]
+    f32 = [GaugeField.from_array(f, prec="c64") for f in f64]
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    out = {"fields": len(dims), "sites": sites, "gen_s": gen_s}
+    cands = [(t, b, m) for t in (2, 8, 32) for b in (128, 256) for m in (1, 4)]
+    cfg = E.autotune(f32, candidates=cands, reps=1)
+    b2s = {}
+    for name, fs, nrep in (("fp32", f32, steps), ("fp64", f64, 1)):
+        ens = E.Ensemble(fs, tile=cfg[0], block=cfg[1], blocks_per_sm=cfg[2])
+        ens.capture()
+        ens.launch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(nrep):
+            ens.launch()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / nrep
+        b2 = ens.out[:, 4].cpu().numpy()
+        b2s[name] = b2
+        out[name] = {"ms_per_eval": ms, "sites_per_s": sites / (ms * 1e-3), "fields_per_s": len(dims) / (ms * 1e-3),
+                     "items": ens.items, "config": {"tile_cols": cfg[0], "block": cfg[1], "blocks_per_sm": cfg[2]},
+                     "b2_first": float(b2[0]), "launches_per_eval": 3}
+        ens.close()
+    out["b2_rel_fp32_fp64_max"] = float(max(abs(a - b) / abs(b) for a, b in zip(b2s["fp32"], b2s["fp64"])))
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -411,6 +454,10 @@ def main():
         "clocks": clk,
         "cpu_baseline": cpu,
     }
+    if args.ensemble and rank == 0:
+        del f64, f32, d32, w32, g32
+        torch.cuda.empty_cache()
+        line["ensemble"] = ensemble_bench(max(3, min(args.steps, 10)))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if wsz > 1:

@@ -102,6 +102,12 @@ SIGNATURES = {
     "flue_uzerobar_c": ([_P, _I, _I, _I, _I, _P, _P], _I),
     "flue_magnetic_force_c": ([_P, _I, _I, _I, _I, _I, _I, _I, _P, _P], _I),
     "flue_release_host_cache": ([], None),
+    "flue_ensemble_create": ([_P, _FP, _I, _I, _I, _I, _I], _I),
+    "flue_ensemble_items": ([_P], _I),
+    "flue_ensemble_run": ([_P, _P, _P], _I),
+    "flue_ensemble_capture": ([_P, _P], _I),
+    "flue_ensemble_replay": ([_P, _P], _I),
+    "flue_ensemble_destroy": ([_P], _I),
 }
 
 _lock = threading.Lock()

@@ -88,6 +88,26 @@ def random_field(dims, eps: float, seed: int, device=None):
     return _to_fortran_field(_reunitarise_np(u))
 
 
+def random_field_philox(dims, eps: float, seed: int, device="cuda", prec="c128"):
+    """Like :func:`random_field` but with the Gell-Mann coefficients drawn on
+    the GPU from torch's Philox generator seeded with ``seed`` (for large
+    ensembles, where host generation would dominate).  Deterministic for a
+    given seed and torch build; not the same numbers as the PCG64 path."""
+    import torch
+
+    from .field import GaugeField
+
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    c = torch.randn(_shape(dims) + (8,), generator=g, device=device, dtype=torch.float64)
+    lam = torch.as_tensor(GELL_MANN, device=device)
+    h = torch.einsum("...a,aij->...ij", c.to(torch.complex128), lam) * 0.5
+    del c
+    u = torch.linalg.matrix_exp(1j * eps * h)
+    del h
+    return GaugeField.from_array(u, prec=prec, reunitarise=True)
+
+
 def haar_field(dims, seed: int, device=None):
     rng = np.random.Generator(np.random.PCG64(seed))
     z = (rng.standard_normal(_shape(dims) + (3, 3)) + 1j * rng.standard_normal(_shape(dims) + (3, 3))) / np.sqrt(2)

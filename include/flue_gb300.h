@@ -181,6 +181,28 @@ int flue_meanlink(const flue_field *U, const void *G, int g_dtype, double *d_sum
  * field must be FLUE_C128 or FLUE_C64. */
 int flue_wflow_step(const flue_field *U, double eps, void *ws, size_t ws_bytes, void *stream);
 
+/* ---- ensemble batching (no reference counterpart; the reference's
+ * magnetic app loops over configurations one by one, app/magnetic.f90:109-140)
+ *
+ * Plaquettes, Polyakov loop and B^2 of up to thousands of device fields of
+ * uneven volume (all of one precision) in ONE persistent launch: each field
+ * is cut into items of tile_cols time columns, a grid of blocks_per_sm x SM
+ * blocks of `block` threads (128 or 256) takes items from an atomic counter
+ * (no block waits on another), a finisher sums each field's items in order.
+ * Per field the output holds 6 doubles: sum Re Tr P over spatial planes, over
+ * temporal planes, sum Re Tr and Im Tr of the Polyakov loop, B^2 (divided by
+ * V; 0 when with_b2 = 0), V.  create() allocates the work list and partials
+ * on the current device (library-owned); capture() records memset + kernel +
+ * finisher writing to d_out into a CUDA graph, replay() launches it. */
+typedef struct flue_ensemble flue_ensemble;
+int flue_ensemble_create(flue_ensemble **e, const flue_field *fields, int nfields, int tile_cols, int block,
+                         int blocks_per_sm, int with_b2);
+int flue_ensemble_items(const flue_ensemble *e);
+int flue_ensemble_run(flue_ensemble *e, double *d_out, void *stream);
+int flue_ensemble_capture(flue_ensemble *e, double *d_out);
+int flue_ensemble_replay(flue_ensemble *e, void *stream);
+int flue_ensemble_destroy(flue_ensemble *e);
+
 /* Allocation-free plaquette.  No counterpart in the reference.  Same result
  * as flue_plaquette (same kernel, bitwise the same sum) but without a
  * workspace argument: the per-block partial sums live in an 8 KiB array that

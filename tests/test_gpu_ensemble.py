@@ -1,0 +1,65 @@
+"""Ensemble batching on the GPU: one persistent, graph-captured launch over
+fields of uneven volume against the oracle, field by field."""
+import numpy as np
+import pytest
+
+import oracle
+from flue_gb300 import ensemble, generate
+from flue_gb300.field import GaugeField
+
+pytestmark = pytest.mark.gpu
+
+DIMS = [(4, 4, 4, 4), (6, 4, 4, 4), (8, 6, 6, 6), (5, 3, 4, 6), (4, 6, 6, 6), (3, 2, 3, 2)]
+
+
+@pytest.fixture(scope="module")
+def fields_np():
+    return [generate.random_field(d, 0.4, 100 + i) for i, d in enumerate(DIMS)]
+
+
+def _check(raw, fields_np, tol_sum, tol_b2):
+    for row, U in zip(raw, fields_np):
+        sp = oracle.plaquette(U, 2, 4, 4)[0]
+        tp = oracle.plaquette(U, 1, 1, 4)[0]
+        assert abs(row[0] - sp) <= tol_sum * abs(sp)
+        assert abs(row[1] - tp) <= tol_sum * abs(tp)
+        if U.shape[0] >= 3:
+            assert abs(row[2] - oracle.polyakov(U)[0]) <= tol_sum * U[0].size / 36 * 3
+        assert abs(row[4] - oracle.magnetic(U)) <= tol_b2 * abs(row[4])
+        assert row[5] == np.prod(U.shape[:4])
+
+
+@pytest.mark.parametrize("tile,block,bps", [(1, 128, 1), (4, 256, 2), (16, 256, 4)])
+def test_ensemble_fp64_vs_oracle(fields_np, tile, block, bps):
+    fs = [GaugeField.from_array(U) for U in fields_np]
+    ens = ensemble.Ensemble(fs, tile=tile, block=block, blocks_per_sm=bps)
+    direct = ens.run(graph=False).copy()
+    graphed = ens.run(graph=True)
+    again = ens.run(graph=True)
+    assert np.array_equal(direct, graphed) and np.array_equal(graphed, again)
+    _check(graphed, fields_np, 1e-12, 1e-12)
+
+
+@pytest.mark.parametrize("prec", ["c64", "r12"])
+def test_ensemble_fp32(fields_np, prec):
+    fs = [GaugeField.from_array(U, prec=prec) for U in fields_np]
+    raw = ensemble.Ensemble(fs, tile=2).run()
+    _check(raw, fields_np, 3e-6, 1e-4)
+
+
+def test_autotune_and_observables(fields_np, tmp_path, monkeypatch):
+    monkeypatch.setenv("FLUE_CACHE_DIR", str(tmp_path))
+    fs = [GaugeField.from_array(U) for U in fields_np]
+    cands = [(1, 128, 1), (4, 256, 2)]
+    best = ensemble.autotune(fs, candidates=cands)
+    assert tuple(best) in cands
+    assert ensemble.autotune(fs, candidates=cands) == tuple(best)  # served from the cache
+    obs = ensemble.Ensemble(fs, tile=best[0], block=best[1], blocks_per_sm=best[2]).observables()
+    for o, U in zip(obs, fields_np):
+        s, n = oracle.plaquette(U, 1, 4, 4)
+        assert abs(o["plaq"] - s / n / 3) < 1e-12
+
+
+def test_mixed_precision_rejected(fields_np):
+    with pytest.raises(TypeError):
+        ensemble.Ensemble([GaugeField.from_array(fields_np[0]), GaugeField.from_array(fields_np[1], prec="c64")])
