@@ -395,6 +395,208 @@ struct MatPlanes {
     }
 };
 
+// Pipeline intermediates, one matrix per (plane k, site s) stored contiguously
+// so that a thread fetches it with 128-bit loads from a single address:
+// FP32 18 reals padded to 5 float4 (80 B), FP64 18 reals as 9 double2
+// (144 B).  A warp reading 32 consecutive sites still touches one contiguous
+// 2.5 / 4.5 KB range, so every sector it fetches is fully used.
+template <typename T>
+struct MatAoS;
+template <>
+struct MatAoS<float> {
+    float4* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ M3<float> load(int64_t s, int k) const {
+        const float4* q = p + ((int64_t)k * V + s) * 5;
+        M3<float> m;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 v = q[j];
+            m.r[2 * j] = v.x;
+            m.i[2 * j] = v.y;
+            m.r[2 * j + 1] = v.z;
+            m.i[2 * j + 1] = v.w;
+        }
+        const float4 v = q[4];
+        m.r[8] = v.x;
+        m.i[8] = v.y;
+        return m;
+    }
+    __device__ __forceinline__ void store(int64_t s, int k, const M3<float>& m) const {
+        float4* q = p + ((int64_t)k * V + s) * 5;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) q[j] = make_float4(m.r[2 * j], m.i[2 * j], m.r[2 * j + 1], m.i[2 * j + 1]);
+        q[4] = make_float4(m.r[8], m.i[8], 0.f, 0.f);
+    }
+    static constexpr size_t bytes_per_matrix = 80;
+};
+template <>
+struct MatAoS<double> {
+    double2* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ M3<double> load(int64_t s, int k) const {
+        const double2* q = p + ((int64_t)k * V + s) * 9;
+        M3<double> m;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            const double2 v = q[e];
+            m.r[e] = v.x;
+            m.i[e] = v.y;
+        }
+        return m;
+    }
+    __device__ __forceinline__ void store(int64_t s, int k, const M3<double>& m) const {
+        double2* q = p + ((int64_t)k * V + s) * 9;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) q[e] = make_double2(m.r[e], m.i[e]);
+    }
+    static constexpr size_t bytes_per_matrix = 144;
+};
+
+// Anti-Hermitian matrix per (plane k, site s), contiguous: Im F00, Im F11,
+// Im F22, F01, F02, F12 (re, im) -- 9 reals padded to 12 (FP32, 3 float4) or
+// 10 (FP64, 5 double2).
+template <typename T>
+__device__ __forceinline__ M3<T> ah_expand(const T v[9]) {
+    M3<T> m;
+    m.r[0] = m.r[4] = m.r[8] = T(0);
+    m.i[0] = v[0];
+    m.i[4] = v[1];
+    m.i[8] = v[2];
+    m.r[1] = v[3];
+    m.i[1] = v[4];
+    m.r[3] = -v[3];
+    m.i[3] = v[4];
+    m.r[2] = v[5];
+    m.i[2] = v[6];
+    m.r[6] = -v[5];
+    m.i[6] = v[6];
+    m.r[5] = v[7];
+    m.i[5] = v[8];
+    m.r[7] = -v[7];
+    m.i[7] = v[8];
+    return m;
+}
+// Products with an anti-Hermitian K given as its 9 packed reals (Im K00,
+// Im K11, Im K22, K01, K02, K12): the real diagonal is zero, so each output
+// element costs 10 FMA instead of 12.
+template <typename T>
+__device__ __forceinline__ T ahr(const T v[9], int a, int c) {  // Re K_ac
+    return (a == c) ? T(0)
+           : (a == 0 && c == 1) ? v[3]
+           : (a == 0 && c == 2) ? v[5]
+           : (a == 1 && c == 2) ? v[7]
+           : (a == 1 && c == 0) ? -v[3]
+           : (a == 2 && c == 0) ? -v[5]
+                                : -v[7];
+}
+template <typename T>
+__device__ __forceinline__ T ahi(const T v[9], int a, int c) {  // Im K_ac
+    return (a == c) ? v[a] : ((a + c) == 1) ? v[4] : ((a + c) == 2) ? v[6] : v[8];
+}
+// C += K X
+template <typename T>
+__device__ __forceinline__ void mac_kx(M3<T>& C, const T k[9], const M3<T>& X) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            T re = C.r[3 * a + b], im = C.i[3 * a + b];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T xr = X.r[3 * c + b], xi = X.i[3 * c + b];
+                const T ki = ahi(k, a, c);
+                if (a != c) {
+                    const T kr = ahr(k, a, c);
+                    re = fma(kr, xr, re);
+                    im = fma(kr, xi, im);
+                }
+                re = fma(-ki, xi, re);
+                im = fma(ki, xr, im);
+            }
+            C.r[3 * a + b] = re;
+            C.i[3 * a + b] = im;
+        }
+}
+// C += X K
+template <typename T>
+__device__ __forceinline__ void mac_xk(M3<T>& C, const M3<T>& X, const T k[9]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            T re = C.r[3 * a + b], im = C.i[3 * a + b];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T xr = X.r[3 * a + c], xi = X.i[3 * a + c];
+                const T ki = ahi(k, c, b);
+                if (c != b) {
+                    const T kr = ahr(k, c, b);
+                    re = fma(xr, kr, re);
+                    im = fma(xi, kr, im);
+                }
+                re = fma(-xi, ki, re);
+                im = fma(xr, ki, im);
+            }
+            C.r[3 * a + b] = re;
+            C.i[3 * a + b] = im;
+        }
+}
+
+template <typename T>
+struct AHAoS;
+template <>
+struct AHAoS<float> {
+    float4* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ void load_packed(int64_t s, int k, float v[9]) const {
+        const float4* q = p + ((int64_t)k * V + s) * 3;
+        const float4 a = q[0], b = q[1], c = q[2];
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w;
+        v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+        v[8] = c.x;
+    }
+    __device__ __forceinline__ M3<float> load(int64_t s, int k) const {
+        const float4* q = p + ((int64_t)k * V + s) * 3;
+        const float4 a = q[0], b = q[1], c = q[2];
+        const float v[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+        return ah_expand<float>(v);
+    }
+    __device__ __forceinline__ void store(int64_t s, int k, const M3<float>& m) const {
+        float4* q = p + ((int64_t)k * V + s) * 3;
+        q[0] = make_float4(m.i[0], m.i[4], m.i[8], m.r[1]);
+        q[1] = make_float4(m.i[1], m.r[2], m.i[2], m.r[5]);
+        q[2] = make_float4(m.i[5], 0.f, 0.f, 0.f);
+    }
+    static constexpr size_t bytes_per_matrix = 48;
+};
+template <>
+struct AHAoS<double> {
+    double2* __restrict__ p;
+    int64_t V;
+    __device__ __forceinline__ void load_packed(int64_t s, int k, double v[9]) const {
+        const double2* q = p + ((int64_t)k * V + s) * 5;
+        const double2 a = q[0], b = q[1], c = q[2], d = q[3], e = q[4];
+        v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y, v[4] = c.x;
+        v[5] = c.y, v[6] = d.x, v[7] = d.y, v[8] = e.x;
+    }
+    __device__ __forceinline__ M3<double> load(int64_t s, int k) const {
+        const double2* q = p + ((int64_t)k * V + s) * 5;
+        const double2 a = q[0], b = q[1], c = q[2], d = q[3], e = q[4];
+        const double v[9] = {a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x};
+        return ah_expand<double>(v);
+    }
+    __device__ __forceinline__ void store(int64_t s, int k, const M3<double>& m) const {
+        double2* q = p + ((int64_t)k * V + s) * 5;
+        q[0] = make_double2(m.i[0], m.i[4]);
+        q[1] = make_double2(m.i[8], m.r[1]);
+        q[2] = make_double2(m.i[1], m.r[2]);
+        q[3] = make_double2(m.i[2], m.r[5]);
+        q[4] = make_double2(m.i[5], 0.0);
+    }
+    static constexpr size_t bytes_per_matrix = 80;
+};
+
 // Anti-Hermitian matrices stored as 9 reals per site: Im F00, Im F11, Im F22,
 // F01 (re, im), F02 (re, im), F12 (re, im) at base[(k*9 + e)*V + s].
 template <typename T>

@@ -98,9 +98,38 @@ __device__ __forceinline__ int64_t dsp(const Geom& g, int mu, int cmu, int k) {
 
 __device__ __forceinline__ int wrapd(int c, int k, int n) {
     int t = c + k;
-    while (t < 0) t += n;
-    while (t >= n) t -= n;
+    if (n > 3) {  // every stencil offset is within +-3: one conditional wrap
+        t += (t < 0) ? n : 0;
+        t -= (t >= n) ? n : 0;
+    } else {
+        while (t < 0) t += n;
+        while (t >= n) t -= n;
+    }
     return t - c;
+}
+
+// Traversal order of the site blocks of the stencil kernels.  The lattice is
+// a sequence of rows (fixed y, z) of NT*NX sites.  When a row holds a whole
+// number of blocks and NY, NZ are multiples of the tile, rows are visited in
+// TILE x TILE (y,z) tiles, y fastest, so that the blocks in flight cover a
+// compact neighbourhood and the +-3 halo they read is still in L2.
+#ifndef FLUE_TILE_YZ
+#define FLUE_TILE_YZ 0
+#endif
+__device__ __forceinline__ int64_t site_block(int64_t b, const Geom& g, int bs) {
+#if FLUE_TILE_YZ > 0
+    const int T = FLUE_TILE_YZ;
+    const int64_t rowlen = (int64_t)g.n[0] * g.n[1];
+    if (rowlen % bs == 0 && g.n[2] % T == 0 && g.n[3] % T == 0) {
+        const int64_t bpr = rowlen / bs;
+        const int64_t in_row = b % bpr, row = b / bpr;
+        const int64_t tile = row / (T * T), r = row % (T * T);
+        const int64_t nty = g.n[2] / T;
+        const int64_t y = (tile % nty) * T + r % T, z = (tile / nty) * T + r / T;
+        return (y + (int64_t)g.n[2] * z) * bpr + in_row;
+    }
+#endif
+    return b;
 }
 
 // Per-thread view of one plane (mu,nu) around the thread's site: every
@@ -108,7 +137,7 @@ __device__ __forceinline__ int wrapd(int c, int k, int n) {
 // arrays, so nothing lands in local memory).
 template <typename T>
 struct Ctx {
-    MatPlanes<T> lines;  // 3 per slot: L^1 (U expanded), L^2, L^3
+    MatAoS<T> lines;  // 3 per slot: L^1 (U expanded), L^2, L^3
     int64_t s;
     int cm, cn, nm, nn;  // coordinates and extents along mu, nu
     int64_t stm, stn;    // site strides along mu, nu
@@ -130,7 +159,7 @@ struct Ctx {
 };
 
 template <typename T>
-__device__ __forceinline__ Ctx<T> make_ctx(const MatPlanes<T>& lines, const Geom& g, int64_t s, const int c[4], int mu,
+__device__ __forceinline__ Ctx<T> make_ctx(const MatAoS<T>& lines, const Geom& g, int64_t s, const int c[4], int mu,
                                            int nu, int smu, int snu) {
     Ctx<T> cx;
     cx.lines = lines;
@@ -164,7 +193,7 @@ __device__ __forceinline__ void corner_off(int k, int a, int b, int& di, int& dj
 //    L^3_d(y) = L^2_d(y) U_d(y+2d)
 // ---------------------------------------------------------------------------
 template <class L, typename T>
-__global__ void k_lines(L U, Geom g, PlaneArg pa, MatPlanes<T> lines) {
+__global__ void k_lines(L U, Geom g, PlaneArg pa, MatAoS<T> lines) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     const int slot = blockIdx.y;
@@ -194,23 +223,33 @@ __global__ void k_lines(L U, Geom g, PlaneArg pa, MatPlanes<T> lines) {
 #define FLUE_FWD_BS 128
 #endif
 #ifndef FLUE_FWD_MINB
-#define FLUE_FWD_MINB 1
+#define FLUE_FWD_MINB 3
 #endif
 #ifndef FLUE_COT_BS
 #define FLUE_COT_BS 128
 #endif
 #ifndef FLUE_COT_MINB
-#define FLUE_COT_MINB 1
+#define FLUE_COT_MINB 4
 #endif
+// the register caps apply to the FP32 kernels; the FP64 ones keep every
+// register they need (they are bound by the FP64 pipe, not by latency)
+template <typename T>
+struct MinBlocks {
+    static constexpr int fwd = 1, cot = 1;
+};
+template <>
+struct MinBlocks<float> {
+    static constexpr int fwd = FLUE_FWD_MINB, cot = FLUE_COT_MINB;
+};
 constexpr int FWD_BS = FLUE_FWD_BS;
 
 template <typename T>
-__global__ void __launch_bounds__(FWD_BS, FLUE_FWD_MINB)
-    k_fwd(Geom g, PlaneArg pa, int kind, MatPlanes<T> lines, AHPlanes<T> kout, RefOut<T> fout, double* part) {
+__global__ void __launch_bounds__(FWD_BS, MinBlocks<T>::fwd)
+    k_fwd(Geom g, PlaneArg pa, int kind, MatAoS<T> lines, AHAoS<T> kout, RefOut<T> fout, double* part) {
     __shared__ double sh[32];
     // planes of the same site block run in adjacent blocks (L2 reuse)
     const int p = blockIdx.x % pa.np;
-    const int64_t s = (int64_t)(blockIdx.x / pa.np) * blockDim.x + threadIdx.x;
+    const int64_t s = site_block(blockIdx.x / pa.np, g, blockDim.x) * blockDim.x + threadIdx.x;
     double e = 0.0;
     if (s < g.V) {
         int c[4];
@@ -220,21 +259,37 @@ __global__ void __launch_bounds__(FWD_BS, FLUE_FWD_MINB)
         const Shape* shp = kind == 1 ? c_shapes5 : c_shapes1;
         const int nsh = kind == 1 ? 7 : 1;
         M3<T> q = m_zero<T>();
-        // one loop over the 4 * nsh leaves, a single copy of the leaf body
+        // Per shape the four quadrant leaves, with their dagger patterns fixed
+        // at compile time (lines are loaded undaggered; L(i,j) = line at
+        // offset (i mu + j nu)):
+        //   TR = Lm(0,0) Ln(a,0) Lm(0,b)^+ Ln(0,0)^+
+        //   TL = Ln(0,0) Lm(-a,b)^+ Ln(-a,0)^+ Lm(-a,0)
+        //   BL = Lm(-a,0)^+ Ln(-a,-b)^+ Lm(-a,-b) Ln(0,-b)
+        //   BR = Ln(0,-b)^+ Lm(0,-b) Ln(a,-b) Lm(0,0)^+
+        // Lm(0,0), Ln(0,0), Lm(-a,0), Ln(0,-b) serve two leaves each.
 #pragma unroll 1
-        for (int lf = 0; lf < 4 * nsh; ++lf) {
-            const int k = lf >> 2, qd = (lf & 3) + 1;
+        for (int k = 0; k < nsh; ++k) {
             const int a = shp[k].a, b = shp[k].b;
-            int di, dj;
-            corner_off(qd, a, b, di, dj);
-            const int i0 = -di, j0 = -dj;
-            const M3<T> s0 = cx.side(qd, i0, j0, a, b);
-            const M3<T> s1 = cx.side(qd % 4 + 1, i0, j0, a, b);
-            const M3<T> t01 = mul(s0, s1);
-            const M3<T> s2 = cx.side((qd + 1) % 4 + 1, i0, j0, a, b);
-            const M3<T> t012 = mul(t01, s2);
-            const M3<T> s3 = cx.side((qd + 2) % 4 + 1, i0, j0, a, b);
-            M3<T> w = mul(t012, s3);
+            const int km = cx.kmu + a - 1, kn = cx.knu + b - 1;
+            M3<T> w;
+            {
+                const M3<T> m00 = lines.load(cx.at(0, 0), km);
+                const M3<T> n00 = lines.load(cx.at(0, 0), kn);
+                M3<T> t = mm<false, false>(m00, lines.load(cx.at(a, 0), kn));
+                t = mm<false, true>(t, lines.load(cx.at(0, b), km));
+                w = mm<false, true>(t, n00);  // TR
+                const M3<T> ma0 = lines.load(cx.at(-a, 0), km);
+                t = mm<false, true>(n00, lines.load(cx.at(-a, b), km));
+                t = mm<false, true>(t, lines.load(cx.at(-a, 0), kn));
+                mac<false, false>(w, t, ma0);  // TL
+                const M3<T> n0b = lines.load(cx.at(0, -b), kn);
+                t = mm<true, true>(ma0, lines.load(cx.at(-a, -b), kn));
+                t = mm<false, false>(t, lines.load(cx.at(-a, -b), km));
+                mac<false, false>(w, t, n0b);  // BL
+                t = mm<true, false>(n0b, lines.load(cx.at(0, -b), km));
+                t = mm<false, false>(t, lines.load(cx.at(a, -b), kn));
+                mac<false, true>(w, t, m00);  // BR
+            }
             m_axpy(q, (T)shp[k].c, w);
         }
         const M3<T> f = ah_quarter(q);
@@ -253,54 +308,50 @@ __global__ void __launch_bounds__(FWD_BS, FLUE_FWD_MINB)
 // ---------------------------------------------------------------------------
 constexpr int COT_BS = FLUE_COT_BS;
 
+// packed anti-Hermitian cotangent K (9 reals) at corner k of the rectangle
 template <typename T>
-__device__ __forceinline__ M3<T> corner_k(const Ctx<T>& cx, const AHPlanes<T>& kin, int p, int k, int i0, int j0, int a,
-                                          int b) {
+__device__ __forceinline__ void corner_k(const Ctx<T>& cx, const AHAoS<T>& kin, int p, int k, int i0, int j0, int a,
+                                         int b, T v[9]) {
     int di, dj;
     corner_off(k, a, b, di, dj);
-    return kin.load(cx.at(i0 + di, j0 + dj), p);
+    kin.load_packed(cx.at(i0 + di, j0 + dj), p, v);
 }
 
 // Sum of the four corner insertions in the word that follows side q of the
 // rectangle (i0,j0,a,b):  Ka A B C + A Kb B C + A B Kc C + A B C Kd with
 // A,B,C = S_q+1, S_q+2, S_q+3 and Ka,Kb,Kc,Kd = K_q+1, K_q+2, K_q+3, K_q.
 template <typename T>
-__device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHPlanes<T>& kin, int p, int q, int i0, int j0, int a,
+__device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHAoS<T>& kin, int p, int q, int i0, int j0, int a,
                                           int b) {
     const int q1 = q % 4 + 1, q2 = q1 % 4 + 1, q3 = q2 % 4 + 1;
+    T kv[9];
     const M3<T> C = cx.side(q3, i0, j0, a, b);
-    M3<T> t1;
-    {
-        const M3<T> kd = corner_k(cx, kin, p, q, i0, j0, a, b);
-        t1 = mul(C, kd);
-        const M3<T> kc = corner_k(cx, kin, p, q3, i0, j0, a, b);
-        mac<false, false>(t1, kc, C);
-    }
+    M3<T> t1 = m_zero<T>();
+    corner_k(cx, kin, p, q, i0, j0, a, b, kv);
+    mac_xk(t1, C, kv);
+    corner_k(cx, kin, p, q3, i0, j0, a, b, kv);
+    mac_kx(t1, kv, C);
     const M3<T> B = cx.side(q2, i0, j0, a, b);
     const M3<T> bc = mul(B, C);
     M3<T> t2 = mul(B, t1);
-    {
-        const M3<T> kb = corner_k(cx, kin, p, q2, i0, j0, a, b);
-        mac<false, false>(t2, kb, bc);
-    }
+    corner_k(cx, kin, p, q2, i0, j0, a, b, kv);
+    mac_kx(t2, kv, bc);
     const M3<T> A = cx.side(q1, i0, j0, a, b);
     const M3<T> abc = mul(A, bc);
     M3<T> res = mul(A, t2);
-    {
-        const M3<T> ka = corner_k(cx, kin, p, q1, i0, j0, a, b);
-        mac<false, false>(res, ka, abc);
-    }
+    corner_k(cx, kin, p, q1, i0, j0, a, b, kv);
+    mac_kx(res, kv, abc);
     return res;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(COT_BS, FLUE_COT_MINB)
-    k_linecot(Geom g, PlaneArg pa, MatPlanes<T> lines, AHPlanes<T> kin, MatPlanes<T> lam) {
+__global__ void __launch_bounds__(COT_BS, MinBlocks<T>::cot)
+    k_linecot(Geom g, PlaneArg pa, MatAoS<T> lines, AHAoS<T> kin, MatAoS<T> lam) {
     // the 3 * nd (direction, length) tasks of one site block run in adjacent
     // blocks, so the neighbourhood they all read stays in L2
     const int ntask = 3 * pa.nd;
     const int task = blockIdx.x % ntask;
-    const int64_t s = (int64_t)(blockIdx.x / ntask) * blockDim.x + threadIdx.x;
+    const int64_t s = site_block(blockIdx.x / ntask, g, blockDim.x) * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     const int slot = task / 3;
     const int len = task % 3 + 1;
@@ -340,7 +391,7 @@ __global__ void __launch_bounds__(COT_BS, FLUE_COT_MINB)
 // 4. link cotangents and gradient output: one thread per (site, direction)
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_linkcot(Geom g, PlaneArg pa, MatPlanes<T> lines, MatPlanes<T> lam, T scale, int form, RefOut<T> out) {
+__global__ void k_linkcot(Geom g, PlaneArg pa, MatAoS<T> lines, MatAoS<T> lam, T scale, int form, RefOut<T> out) {
     const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (z >= g.V) return;
     const int d = blockIdx.y;
@@ -406,13 +457,15 @@ struct EnergyWs {
 };
 
 static EnergyWs energy_layout(const Geom& g, int prec, const PlaneArg& pa, bool with_force) {
-    const size_t cs = prec == PREC_C128 ? 8 : 4;  // real size of compute type
+    const bool d = prec == PREC_C128;  // FP64 intermediates
+    const size_t mat = d ? MatAoS<double>::bytes_per_matrix : MatAoS<float>::bytes_per_matrix;
+    const size_t ah = d ? AHAoS<double>::bytes_per_matrix : AHAoS<float>::bytes_per_matrix;
     EnergyWs w;
     const int nbx = (int)((g.V + FWD_BS - 1) / FWD_BS);
     w.lines = 0;
-    w.kbuf = align256(w.lines + (size_t)3 * pa.nd * 9 * g.V * 2 * cs);
-    w.lam = align256(w.kbuf + (with_force ? (size_t)pa.np * 9 * g.V * cs : 0));
-    w.part = align256(w.lam + (with_force ? (size_t)3 * pa.nd * 9 * g.V * 2 * cs : 0));
+    w.kbuf = align256(w.lines + (size_t)3 * pa.nd * g.V * mat);
+    w.lam = align256(w.kbuf + (with_force ? (size_t)pa.np * g.V * ah : 0));
+    w.part = align256(w.lam + (with_force ? (size_t)3 * pa.nd * g.V * mat : 0));
     w.total = align256(w.part + (size_t)pa.np * nbx * sizeof(double));
     return w;
 }
@@ -466,9 +519,9 @@ template <class L, typename T>
 static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, int kind, double* out_E, void* force,
                                int form, char* ws, const EnergyWs& w, RefOut<T> fout, cudaStream_t st) {
     using C2 = typename V2<T>::type;
-    MatPlanes<T> lines{(C2*)(ws + w.lines), g.V};
-    AHPlanes<T> kb{force ? (T*)(ws + w.kbuf) : nullptr, g.V};
-    MatPlanes<T> lam{(C2*)(ws + w.lam), g.V};
+    MatAoS<T> lines{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lines), g.V};
+    AHAoS<T> kb{force ? reinterpret_cast<decltype(AHAoS<T>::p)>(ws + w.kbuf) : nullptr, g.V};
+    MatAoS<T> lam{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lam), g.V};
     double* part = out_E ? (double*)(ws + w.part) : nullptr;
     const unsigned nbx = (unsigned)((g.V + FWD_BS - 1) / FWD_BS);
     stage_mark(0, st);
