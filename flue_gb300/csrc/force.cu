@@ -324,22 +324,36 @@ template <typename T>
 __device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHAoS<T>& kin, int p, int q, int i0, int j0, int a,
                                           int b) {
     const int q1 = q % 4 + 1, q2 = q1 % 4 + 1, q3 = q2 % 4 + 1;
+    // The rectangle has four distinct sites, its corners c1..c4; every side
+    // starts at one of them (S1 at c1, S2 at c2, S3 = L(c4)^+, S4 = L(c1)^+),
+    // so 4 wrapped coordinates give all 7 operand addresses.
+    const int sm0 = wrapd(cx.cm, i0, cx.nm) * (int)cx.stm, sm1 = wrapd(cx.cm, i0 + a, cx.nm) * (int)cx.stm;
+    const int sn0 = wrapd(cx.cn, j0, cx.nn) * (int)cx.stn, sn1 = wrapd(cx.cn, j0 + b, cx.nn) * (int)cx.stn;
+    const int s0 = (int)cx.s;
+    const int c1 = s0 + sm0 + sn0, c2 = s0 + sm1 + sn0, c3 = s0 + sm1 + sn1, c4 = s0 + sm0 + sn1;
+    auto corner = [&](int k) { return k == 1 ? c1 : (k == 2 ? c2 : (k == 3 ? c3 : c4)); };
+    auto side = [&](int k) {
+        const int site = (k == 2) ? c2 : (k == 3 ? c4 : c1);
+        const int plane = (k & 1) ? cx.kmu + a - 1 : cx.knu + b - 1;
+        const M3<T> m = cx.lines.load(site, plane);
+        return k >= 3 ? dag(m) : m;
+    };
     T kv[9];
-    const M3<T> C = cx.side(q3, i0, j0, a, b);
+    const M3<T> C = side(q3);
     M3<T> t1 = m_zero<T>();
-    corner_k(cx, kin, p, q, i0, j0, a, b, kv);
+    kin.load_packed(corner(q), p, kv);
     mac_xk(t1, C, kv);
-    corner_k(cx, kin, p, q3, i0, j0, a, b, kv);
+    kin.load_packed(corner(q3), p, kv);
     mac_kx(t1, kv, C);
-    const M3<T> B = cx.side(q2, i0, j0, a, b);
+    const M3<T> B = side(q2);
     const M3<T> bc = mul(B, C);
     M3<T> t2 = mul(B, t1);
-    corner_k(cx, kin, p, q2, i0, j0, a, b, kv);
+    kin.load_packed(corner(q2), p, kv);
     mac_kx(t2, kv, bc);
-    const M3<T> A = cx.side(q1, i0, j0, a, b);
+    const M3<T> A = side(q1);
     const M3<T> abc = mul(A, bc);
     M3<T> res = mul(A, t2);
-    corner_k(cx, kin, p, q1, i0, j0, a, b, kv);
+    kin.load_packed(corner(q1), p, kv);
     mac_kx(res, kv, abc);
     return res;
 }
