@@ -113,6 +113,11 @@ __device__ __forceinline__ int wrapd(int c, int k, int n) {
 // number of blocks and NY, NZ are multiples of the tile, rows are visited in
 // TILE x TILE (y,z) tiles, y fastest, so that the blocks in flight cover a
 // compact neighbourhood and the +-3 halo they read is still in L2.
+// FLUE_LINES_DAG = 1 keeps daggered copies of the lines so that the line
+// cotangents need no select instructions for S3, S4 (twice the line storage)
+#ifndef FLUE_LINES_DAG
+#define FLUE_LINES_DAG 0
+#endif
 #ifndef FLUE_TILE_YZ
 #define FLUE_TILE_YZ 0
 #endif
@@ -211,7 +216,15 @@ __global__ void k_lines(L U, Geom g, PlaneArg pa, MatAoS<T> lines) {
     const M3<T> l2 = mul(u0, U.load(s1, d));
     lines.store(s, 3 * slot, u0);
     lines.store(s, 3 * slot + 1, l2);
-    lines.store(s, 3 * slot + 2, mul(l2, U.load(s2, d)));
+    const M3<T> l3 = mul(l2, U.load(s2, d));
+    lines.store(s, 3 * slot + 2, l3);
+#if FLUE_LINES_DAG
+    // daggered copies after the 3 * nd plain lines (the line cotangents read
+    // S3, S4 = L^+ without select instructions)
+    lines.store(s, 3 * (pa.nd + slot), dag(u0));
+    lines.store(s, 3 * (pa.nd + slot) + 1, dag(l2));
+    lines.store(s, 3 * (pa.nd + slot) + 2, dag(l3));
+#endif
 }
 
 // ---------------------------------------------------------------------------
@@ -271,23 +284,27 @@ __global__ void __launch_bounds__(FWD_BS, MinBlocks<T>::fwd)
         for (int k = 0; k < nsh; ++k) {
             const int a = shp[k].a, b = shp[k].b;
             const int km = cx.kmu + a - 1, kn = cx.knu + b - 1;
+            // the 3 x 3 sites (i, j) in {-a, 0, a} x {-b, 0, b} the leaves use
+            const int s0 = (int)cx.s, stm = (int)cx.stm, stn = (int)cx.stn;
+            const int mM = wrapd(cx.cm, -a, cx.nm) * stm, mP = wrapd(cx.cm, a, cx.nm) * stm;
+            const int nM = wrapd(cx.cn, -b, cx.nn) * stn, nP = wrapd(cx.cn, b, cx.nn) * stn;
             M3<T> w;
             {
-                const M3<T> m00 = lines.load(cx.at(0, 0), km);
-                const M3<T> n00 = lines.load(cx.at(0, 0), kn);
-                M3<T> t = mm<false, false>(m00, lines.load(cx.at(a, 0), kn));
-                t = mm<false, true>(t, lines.load(cx.at(0, b), km));
+                const M3<T> m00 = lines.load(s0, km);
+                const M3<T> n00 = lines.load(s0, kn);
+                M3<T> t = mm<false, false>(m00, lines.load(s0 + mP, kn));
+                t = mm<false, true>(t, lines.load(s0 + nP, km));
                 w = mm<false, true>(t, n00);  // TR
-                const M3<T> ma0 = lines.load(cx.at(-a, 0), km);
-                t = mm<false, true>(n00, lines.load(cx.at(-a, b), km));
-                t = mm<false, true>(t, lines.load(cx.at(-a, 0), kn));
+                const M3<T> ma0 = lines.load(s0 + mM, km);
+                t = mm<false, true>(n00, lines.load(s0 + mM + nP, km));
+                t = mm<false, true>(t, lines.load(s0 + mM, kn));
                 mac<false, false>(w, t, ma0);  // TL
-                const M3<T> n0b = lines.load(cx.at(0, -b), kn);
-                t = mm<true, true>(ma0, lines.load(cx.at(-a, -b), kn));
-                t = mm<false, false>(t, lines.load(cx.at(-a, -b), km));
+                const M3<T> n0b = lines.load(s0 + nM, kn);
+                t = mm<true, true>(ma0, lines.load(s0 + mM + nM, kn));
+                t = mm<false, false>(t, lines.load(s0 + mM + nM, km));
                 mac<false, false>(w, t, n0b);  // BL
-                t = mm<true, false>(n0b, lines.load(cx.at(0, -b), km));
-                t = mm<false, false>(t, lines.load(cx.at(a, -b), kn));
+                t = mm<true, false>(n0b, lines.load(s0 + nM, km));
+                t = mm<false, false>(t, lines.load(s0 + mP + nM, kn));
                 mac<false, true>(w, t, m00);  // BR
             }
             m_axpy(q, (T)shp[k].c, w);
@@ -322,7 +339,7 @@ __device__ __forceinline__ void corner_k(const Ctx<T>& cx, const AHAoS<T>& kin, 
 // A,B,C = S_q+1, S_q+2, S_q+3 and Ka,Kb,Kc,Kd = K_q+1, K_q+2, K_q+3, K_q.
 template <typename T>
 __device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHAoS<T>& kin, int p, int q, int i0, int j0, int a,
-                                          int b) {
+                                          int b, int dagoff) {
     const int q1 = q % 4 + 1, q2 = q1 % 4 + 1, q3 = q2 % 4 + 1;
     // The rectangle has four distinct sites, its corners c1..c4; every side
     // starts at one of them (S1 at c1, S2 at c2, S3 = L(c4)^+, S4 = L(c1)^+),
@@ -334,9 +351,14 @@ __device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHAoS<T>& kin,
     auto corner = [&](int k) { return k == 1 ? c1 : (k == 2 ? c2 : (k == 3 ? c3 : c4)); };
     auto side = [&](int k) {
         const int site = (k == 2) ? c2 : (k == 3 ? c4 : c1);
+#if FLUE_LINES_DAG
+        const int plane = ((k & 1) ? cx.kmu + a - 1 : cx.knu + b - 1) + (k >= 3 ? dagoff : 0);
+        return cx.lines.load(site, plane);
+#else
         const int plane = (k & 1) ? cx.kmu + a - 1 : cx.knu + b - 1;
         const M3<T> m = cx.lines.load(site, plane);
         return k >= 3 ? dag(m) : m;
+#endif
     };
     T kv[9];
     const M3<T> C = side(q3);
@@ -390,7 +412,7 @@ __global__ void __launch_bounds__(COT_BS, MinBlocks<T>::cot)
             if ((is_mu ? a : b) != len) continue;
             const int q = is_mu ? (second ? 3 : 1) : (second ? 4 : 2);
             const int i0 = (q == 2) ? -a : 0, j0 = (q == 3) ? -b : 0;
-            const M3<T> r = side_cot(cx, kin, p, q, i0, j0, a, b);
+            const M3<T> r = side_cot(cx, kin, p, q, i0, j0, a, b, 3 * pa.nd);
             const T coef = (T)c_shapes5[k].c;
             if (second)
                 m_axpy_dag(acc, coef, r);
@@ -477,7 +499,7 @@ static EnergyWs energy_layout(const Geom& g, int prec, const PlaneArg& pa, bool 
     EnergyWs w;
     const int nbx = (int)((g.V + FWD_BS - 1) / FWD_BS);
     w.lines = 0;
-    w.kbuf = align256(w.lines + (size_t)3 * pa.nd * g.V * mat);
+    w.kbuf = align256(w.lines + (size_t)(FLUE_LINES_DAG ? 6 : 3) * pa.nd * g.V * mat);
     w.lam = align256(w.kbuf + (with_force ? (size_t)pa.np * g.V * ah : 0));
     w.part = align256(w.lam + (with_force ? (size_t)3 * pa.nd * g.V * mat : 0));
     w.total = align256(w.part + (size_t)pa.np * nbx * sizeof(double));
