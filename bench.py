@@ -64,6 +64,15 @@ def parse():
     return p.parse_args()
 
 
+def bench_config(args, dims, n_replicas):
+    """The workload description shared by both arms of the benchmark."""
+    nt, nx, ny, nz = dims
+    return {"workload": f"5-loop F_munu + B^2 forward + backward (su(3) gradient), {nx}^3x{nt}",
+            "lattice": [nt, nx, ny, nz], "sites": nt * nx * ny * nz, "field_format": args.prec, "eps": args.eps,
+            "seed": args.seed, "global_batch": n_replicas, "parallelism": f"replicas x{n_replicas}",
+            "l2": "inputs and intermediates larger than L2 (field 0.4-0.6 GB, 3 GB scratch per step)"}
+
+
 def ensemble_bench(steps: int):
     """96 fields: L in {16,24,32} x T in {32,48,64}, 8 each, plus 24 at 24^3x48,
     eps = 0.4, per-field seeds (GPU Philox); FP32 (c64) and FP64 (c128)."""
@@ -242,8 +251,7 @@ def run_reference(args, dims, ws, rank):
     line = {"metric": METRIC, "value": val, "unit": "sites/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"magnetic() B^2 forward, {nx}^3x{nt}", "global_batch": 1, "seq_len": None,
-                       "parallelism": "host OpenMP", "eps": args.eps, "seed": args.seed},
+            "config": bench_config(args, dims, 1),
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": "sites/s", "cores": oracle.num_threads(), "kind": "port",
                              "sample": f"per step: time slices 1..{nsl} of the field ({nsl * V3} sites), forward only "
@@ -432,10 +440,7 @@ def main():
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"5-loop F_munu + B^2 forward + backward (su(3) gradient), {nx}^3x{nt}",
-                   "lattice": [nt, nx, ny, nz], "sites": V, "field_format": args.prec, "eps": args.eps,
-                   "seed": args.seed, "global_batch": wsz, "parallelism": f"replicas x{wsz}",
-                   "l2": "inputs and intermediates larger than L2 (field 0.4-0.6 GB, 2.5 GB scratch per step)"},
+        "config": bench_config(args, dims, wsz),
         "fp64": {"value": value64, "unit": "sites/s", "ms_per_step": ms64, "steps": args.fp64_steps},
         "fp32_over_fp64": value / value64,
         "fp32_error_vs_fp64": {"b2_rel": rel_b, "grad_rel_l2": rel_g, "grad_rel_max": gmax, "b2_fp64": B64},

@@ -62,3 +62,18 @@ def test_validation_before_cuda():
     assert L.flue_magnetic_force(ctypes.byref(f4), ctypes.byref(out), None, 0, None, 0, None) == _lib.FLUE_ERR_WORKSPACE
     with pytest.raises(ValueError):
         _lib.call("flue_plaquette", ctypes.byref(f), 1, 4, 4, None, None, 0, None)
+
+
+def test_jackknife_matches_definition():
+    import numpy as np
+
+    from flue_gb300 import jack
+
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(17) + 4.0
+    m, e = jack.mean_and_error(x)
+    assert abs(m - x.mean()) < 1e-14
+    # first-order jackknife error = sqrt((n-1)/n sum (theta_i - theta_bar)^2) = std/sqrt(n) for the mean
+    assert abs(e - x.std(ddof=1) / np.sqrt(x.size)) < 1e-12
+    c2 = jack.complement(x, (3,))
+    assert abs(c2[0] - (x.sum() - x[3] - x[0]) / (x.size - 2)) < 1e-14
