@@ -4,6 +4,7 @@
 // buffers and one stream per device, guarded by a mutex.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -366,7 +367,57 @@ struct DevCache {
     void* out = nullptr;
     size_t out_bytes = 0;
     double* scal = nullptr;
+    // large host<->device copies are split over several streams so that
+    // more than one copy engine moves the bytes
+    static constexpr int kCopyStreams = 4;
+    int ncopy = 1;
+    cudaStream_t cst[kCopyStreams] = {};
+    cudaEvent_t cev[kCopyStreams + 1] = {};
 };
+
+// A device-usable address of host memory `p`, or NULL: pinned (page-locked,
+// mapped) host memory, or -- when the GPU reads through the host's page
+// tables, as GB300 with NVLink-C2C does -- any host memory.  Disabled with
+// FLUE_ZERO_COPY=0.
+static const void* device_view(const void* p) {
+    const char* env = getenv("FLUE_ZERO_COPY");
+    if (env && atoi(env) == 0) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+    int dev = 0, ats = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return ats ? p : nullptr;
+}
+
+// Copy `bytes` between host and device on the cache's stream, as one copy or
+// split into chunks on the copy streams (ordered after everything queued on
+// c->st before the call, and everything queued after it waits for all chunks).
+static cudaError_t copy_async(DevCache* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    const size_t kMinSplit = (size_t)64 << 20;
+    if (c->ncopy <= 1 || bytes < kMinSplit) return cudaMemcpyAsync(dst, src, bytes, kind, c->st);
+    cudaError_t e = cudaEventRecord(c->cev[0], c->st);
+    if (e != cudaSuccess) return e;
+    const size_t chunk = ((bytes / c->ncopy) + 4095) & ~(size_t)4095;
+    for (int k = 0; k < c->ncopy; ++k) {
+        const size_t off = chunk * k;
+        if (off >= bytes) break;
+        const size_t n = (off + chunk > bytes) ? bytes - off : chunk;
+        if ((e = cudaStreamWaitEvent(c->cst[k], c->cev[0], 0)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync((char*)dst + off, (const char*)src + off, n, kind, c->cst[k])) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(c->cev[k + 1], c->cst[k])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(c->st, c->cev[k + 1], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
 
 std::mutex g_cache_mtx;
 std::vector<DevCache*> g_caches;
@@ -404,6 +455,19 @@ DevCache* cache_for_current(int* rc) {
             *rc = cuda_status(e);
             return nullptr;
         }
+        const char* env = getenv("FLUE_COPY_STREAMS");
+        int n = env ? atoi(env) : DevCache::kCopyStreams;
+        c->ncopy = n < 1 ? 1 : (n > DevCache::kCopyStreams ? DevCache::kCopyStreams : n);
+        for (int k = 0; k < DevCache::kCopyStreams && c->ncopy > 1; ++k)
+            if ((e = cudaStreamCreateWithFlags(&c->cst[k], cudaStreamNonBlocking)) != cudaSuccess) {
+                *rc = cuda_status(e);
+                return nullptr;
+            }
+        for (int k = 0; k <= DevCache::kCopyStreams && c->ncopy > 1; ++k)
+            if ((e = cudaEventCreateWithFlags(&c->cev[k], cudaEventDisableTiming)) != cudaSuccess) {
+                *rc = cuda_status(e);
+                return nullptr;
+            }
         c->init = true;
     }
     *rc = FLUE_OK;
@@ -418,7 +482,7 @@ int upload_c128(DevCache* c, const double* data, int nt, int nx, int ny, int nz,
     const size_t bytes = (size_t)flue_field_bytes(nt, nx, ny, nz, FLUE_C128);
     int rc = grow(&c->field, &c->field_bytes, bytes);
     if (rc) return rc;
-    cudaError_t e = cudaMemcpyAsync(c->field, data, bytes, cudaMemcpyHostToDevice, c->st);
+    cudaError_t e = copy_async(c, c->field, data, bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_status(e);
     U->links = c->field;
     U->nt = nt;
@@ -648,23 +712,45 @@ int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int 
     if (!dims_ok(NT, NX, NY, NZ)) return fail(FLUE_ERR_SHAPE, "bad lattice extents");
     HOST_PROLOGUE();
     const size_t in_bytes = (size_t)flue_field_bytes(NT, NX, NY, NZ, data_dtype);
-    if ((rc = grow(&c->field, &c->field_bytes, in_bytes))) return rc;
-    cudaError_t e = cudaMemcpyAsync(c->field, data, in_bytes, cudaMemcpyHostToDevice, c->st);
-    if (e != cudaSuccess) return cuda_status(e);
-    flue_field U = {c->field, NT, NX, NY, NZ, prec};
-    if (prec == FLUE_R12) {
-        const int64_t V = (int64_t)NT * NX * NY * NZ;
-        const int64_t st[7] = {1, NT, (int64_t)NT * NX, (int64_t)NT * NX * NY, V, 4 * V, 12 * V};
-        if ((rc = grow(&c->field2, &c->field2_bytes, (size_t)flue_field_bytes(NT, NX, NY, NZ, FLUE_R12)))) return rc;
-        if ((rc = flue_pack_field(c->field, FLUE_C64, st, NT, NX, NY, NZ, c->field2, FLUE_R12, 0, c->st))) return rc;
+    const int64_t V = (int64_t)NT * NX * NY * NZ;
+    const int64_t st[7] = {1, NT, (int64_t)NT * NX, (int64_t)NT * NX * NY, V, 4 * V, 12 * V};
+    // Zero copy: when the GPU can address the caller's host buffers (pinned
+    // memory, or any memory on a system whose GPU walks the host page tables,
+    // as over NVLink-C2C), the re-layout kernel reads the field straight from
+    // host memory and the gradient kernel writes straight into it -- no
+    // staging copies.  Otherwise the field is copied in and the gradient out.
+    const void* d_in = device_view(data);
+    void* d_grad = grad ? const_cast<void*>(device_view(grad)) : nullptr;
+    flue_field U = {nullptr, NT, NX, NY, NZ, prec};
+    if (d_in) {
+        const size_t fb = (size_t)flue_field_bytes(NT, NX, NY, NZ, prec);
+        if ((rc = grow(&c->field2, &c->field2_bytes, fb))) return rc;
+        if ((rc = flue_pack_field(d_in, data_dtype, st, NT, NX, NY, NZ, c->field2, prec, 0, c->st))) return rc;
         U.links = c->field2;
+    } else {
+        if ((rc = grow(&c->field, &c->field_bytes, in_bytes))) return rc;
+        cudaError_t e = copy_async(c, c->field, data, in_bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_status(e);
+        U.links = c->field;
+        if (prec == FLUE_R12) {
+            if ((rc = grow(&c->field2, &c->field2_bytes, (size_t)flue_field_bytes(NT, NX, NY, NZ, FLUE_R12)))) return rc;
+            if ((rc = flue_pack_field(c->field, FLUE_C64, st, NT, NX, NY, NZ, c->field2, FLUE_R12, 0, c->st))) return rc;
+            U.links = c->field2;
+        }
     }
     if ((rc = ensure_ws(c, FLUE_OP_MAGNETIC_FORCE, U))) return rc;
-    if (grad && (rc = grow(&c->out, &c->out_bytes, in_bytes))) return rc;
-    if ((rc = flue_magnetic_force(&U, c->scal, grad ? c->out : nullptr, force_form, c->ws, c->ws_bytes, c->st)))
-        return rc;
+    void* force_out = nullptr;
     if (grad) {
-        e = cudaMemcpyAsync(grad, c->out, in_bytes, cudaMemcpyDeviceToHost, c->st);
+        if (d_grad) {
+            force_out = d_grad;
+        } else {
+            if ((rc = grow(&c->out, &c->out_bytes, in_bytes))) return rc;
+            force_out = c->out;
+        }
+    }
+    if ((rc = flue_magnetic_force(&U, c->scal, force_out, force_form, c->ws, c->ws_bytes, c->st))) return rc;
+    if (grad && !d_grad) {
+        cudaError_t e = copy_async(c, grad, c->out, in_bytes, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_status(e);
     }
     return fetch(c, B, c->scal, sizeof(double));

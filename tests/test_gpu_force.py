@@ -97,3 +97,30 @@ def test_fp32_force_error_bound(prec):
     g64, g32 = _np(g64), _np(g32).astype(np.complex128)
     assert abs(b32 - b64) / abs(b64) < 1e-6
     assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-5
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_buffer_force_entry(pinned):
+    """flue_magnetic_force_c: host complex64 in, host gradient out (zero-copy
+    when the GPU can address the buffers, staged copies otherwise)."""
+    import ctypes
+
+    from flue_gb300 import _lib
+
+    U = generate.random_field((8, 4, 6, 4), 0.4, 9)
+    f = GaugeField.from_array(U, prec="c64")
+    b_ref, g_ref = forces.magnetic_force(f)
+    host = torch.as_tensor(np.asfortranarray(U.astype(np.complex64))).permute(6, 5, 4, 3, 2, 1, 0).contiguous()
+    grad = torch.zeros_like(host)
+    if pinned:
+        host, grad = host.pin_memory(), grad.pin_memory()
+    L = _lib.load()
+    b = ctypes.c_double()
+    nt, nx, ny, nz = U.shape[:4]
+    for prec in (_lib.C64, _lib.R12):
+        rc = L.flue_magnetic_force_c(ctypes.c_void_p(host.data_ptr()), _lib.C64, nt, nx, ny, nz, prec,
+                                     _lib.FORCE_LIE, ctypes.byref(b), ctypes.c_void_p(grad.data_ptr()))
+        assert rc == 0, L.flue_last_error_detail()
+        assert abs(b.value - b_ref) < 1e-6 * abs(b_ref)
+        g = grad.permute(6, 5, 4, 3, 2, 1, 0).numpy()
+        assert np.abs(g - _np(g_ref)).max() < 1e-5 * np.abs(_np(g_ref)).max()
