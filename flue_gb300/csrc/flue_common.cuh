@@ -429,6 +429,7 @@ struct MatAoS<float> {
         q[4] = make_float4(m.r[8], m.i[8], 0.f, 0.f);
     }
     static constexpr size_t bytes_per_matrix = 80;
+    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 5; }
 };
 template <>
 struct MatAoS<double> {
@@ -451,6 +452,7 @@ struct MatAoS<double> {
         for (int e = 0; e < 9; ++e) q[e] = make_double2(m.r[e], m.i[e]);
     }
     static constexpr size_t bytes_per_matrix = 144;
+    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 9; }
 };
 
 // Anti-Hermitian matrix per (plane k, site s), contiguous: Im F00, Im F11,
@@ -569,6 +571,7 @@ struct AHAoS<float> {
         q[2] = make_float4(m.i[5], 0.f, 0.f, 0.f);
     }
     static constexpr size_t bytes_per_matrix = 48;
+    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 3; }
 };
 template <>
 struct AHAoS<double> {
@@ -595,6 +598,7 @@ struct AHAoS<double> {
         q[4] = make_double2(m.i[5], 0.0);
     }
     static constexpr size_t bytes_per_matrix = 80;
+    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 5; }
 };
 
 // Anti-Hermitian matrices stored as 9 reals per site: Im F00, Im F11, Im F22,
