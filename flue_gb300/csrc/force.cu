@@ -108,16 +108,19 @@ __device__ __forceinline__ int wrapd(int c, int k, int n) {
     return t - c;
 }
 
+// FLUE_LINES_DAG = 1 keeps daggered copies of the lines so that the line
+// cotangents need no select instructions for S3, S4 (twice the line storage;
+// measured slower on GB300, off by default)
+#ifndef FLUE_LINES_DAG
+#define FLUE_LINES_DAG 0
+#endif
+
 // Traversal order of the site blocks of the stencil kernels.  The lattice is
 // a sequence of rows (fixed y, z) of NT*NX sites.  When a row holds a whole
 // number of blocks and NY, NZ are multiples of the tile, rows are visited in
 // TILE x TILE (y,z) tiles, y fastest, so that the blocks in flight cover a
-// compact neighbourhood and the +-3 halo they read is still in L2.
-// FLUE_LINES_DAG = 1 keeps daggered copies of the lines so that the line
-// cotangents need no select instructions for S3, S4 (twice the line storage)
-#ifndef FLUE_LINES_DAG
-#define FLUE_LINES_DAG 0
-#endif
+// compact neighbourhood and the +-3 halo they read is still in L2 (measured
+// no faster on GB300: off by default).
 #ifndef FLUE_TILE_YZ
 #define FLUE_TILE_YZ 0
 #endif
