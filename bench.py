@@ -61,7 +61,87 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--ensemble", action="store_true",
                    help="also time the 96-field ensemble (plaquette/Polyakov/B^2 in one graph-captured launch)")
+    p.add_argument("--observables", action="store_true",
+                   help="instead of the headline step, time every observable entry point (FP64 and FP32-r12)")
     return p.parse_args()
+
+
+# algorithmic bytes per site (links that must be read once + outputs written
+# once) and products per site, per observable, for (c128, r12)
+OBS_COST = {
+    # name: (links read per site, output matrices per site, products per site)
+    "plaquette (6 planes)": (4, 0, 6 * 2.2),
+    "polyakov": (1, 0, 1.0),
+    "wmunu 2x2 (1 plane)": (2, 0, 9.0),
+    "genericpath 8 steps (every site)": (2, 1, 7.0),
+    "clover F (1 plane)": (2, 1, 12.0 + 1),
+    "5-loop F (1 plane)": (2, 1, 84.0 + 4),
+    "magnetic B^2 forward": (3, 0, 252.0 + 6),
+    "B^2 forward+backward": (3, 7, 951.0),
+    "plaquette action + force": (4, 4, 4 * 3 * 4.0),
+    "Wilson-flow RK3 step": (4, 4, 3 * (48.0 + 20)),
+}
+
+
+def observables_bench(dims, steps):
+    """Device time of one call of every observable at `dims`, FP64 (c128) and
+    FP32 (r12), with achieved bandwidth (algorithmic bytes / time) and FLOP rate."""
+    import torch
+
+    from flue_gb300 import flow, forces, generate, gluonCalc as G
+    from flue_gb300.field import GaugeField
+
+    nt, nx, ny, nz = dims
+    V = nt * nx * ny * nz
+    f64 = generate.random_field(dims, 0.3, 1, device="cuda")
+    fields = {"c128": f64, "r12": GaugeField.from_array(f64, prec="r12"), "c64": GaugeField.from_array(f64, prec="c64")}
+    link_b = {"c128": 144, "r12": 48, "c64": 72}
+    mat_b = {"c128": 144, "r12": 72, "c64": 72}
+    path = [2, 2, 3, 3, -2, -2, -3, -3]
+
+    def calls(f):
+        return {
+            "plaquette (6 planes)": lambda: G.plaquette(f, 1, 4, 4),
+            "polyakov": lambda: G.polyakov(f),
+            "wmunu 2x2 (1 plane)": lambda: G.wmunu(f, 2, 3, 2, 2),
+            "genericpath 8 steps (every site)": lambda: G.genericpath_all(f, path),
+            "clover F (1 plane)": lambda: G.cloverloopmunucoord(f, 3, 2),
+            "5-loop F (1 plane)": lambda: G.loop5munucoord(f, 3, 2),
+            "magnetic B^2 forward": lambda: G.magnetic(f),
+            "B^2 forward+backward": lambda: forces.magnetic_force(f),
+            "plaquette action + force": lambda: forces.plaquette_force(f),
+            "Wilson-flow RK3 step": (lambda: flow.wflow_step(f, 0.01)) if f.prec != "r12" else None,
+        }
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    rows = []
+    for prec in ("c128", "c64", "r12"):
+        f = fields[prec]
+        for name, fn in calls(f).items():
+            if fn is None:
+                continue
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            n = steps if name not in ("B^2 forward+backward",) or prec != "c128" else max(1, steps // 5)
+            e0.record()
+            for _ in range(n):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / n
+            lr, mo, pr = OBS_COST[name]
+            byt = V * (lr * link_b[prec] + mo * mat_b[prec])
+            rows.append({"observable": name, "prec": prec, "ms": ms, "sites_per_s": V / (ms * 1e-3),
+                         "alg_GBps": byt / (ms * 1e-3) / 1e9, "hbm_frac": byt / (ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                         "TFLOPs": V * pr * 198 / (ms * 1e-3) / 1e12})
+    return {"lattice": list(dims), "sites": V, "rows": rows,
+            "note": "ms includes the host round trip of scalar results (tiny) and per-call launches; bytes are "
+                    "algorithmic (links read once, outputs written once)"}
 
 
 def bench_config(args, dims, n_replicas):
@@ -282,6 +362,12 @@ def main():
         ws = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))
         run_reference(args, dims, ws, rank)
+        return
+    if args.observables:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(observables_bench(dims, max(3, min(args.steps, 20)))), flush=True)
         return
 
     import numpy as np
