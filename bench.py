@@ -79,7 +79,7 @@ OBS_COST = {
     "magnetic B^2 forward": (3, 0, 252.0 + 6),
     "B^2 forward+backward": (3, 7, 951.0),
     "plaquette action + force": (4, 4, 4 * 3 * 4.0),
-    "Wilson-flow RK3 step": (4, 4, 3 * (48.0 + 20)),
+    "Wilson-flow RK3 step": (4, 4, 3 * (48.0 + 12)),
 }
 
 

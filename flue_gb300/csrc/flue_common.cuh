@@ -256,25 +256,27 @@ __device__ __forceinline__ M3<T> ta_scaled(const M3<T>& m, T s) {
 }
 
 // ---------------------------------------------------------------------------
-// FixSU3Matrix (src/gaugeIO/ILDG_bin.f90:138-151) in FP64 on rows 0 and 1;
-// row 2 becomes conj(row0 x row1) normalised.
+// FixSU3Matrix (src/gaugeIO/ILDG_bin.f90:138-151) on rows 0 and 1; row 2
+// becomes conj(row0 x row1) normalised.  Every caller that restates the
+// reference runs it in FP64; the FP32 Wilson-flow update runs it in float.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void fix_su3_rows(double r[3][3], double i[3][3]) {
+template <typename T>
+__device__ __forceinline__ void fix_su3_rows(T r[3][3], T i[3][3]) {
     // normalise row 0 (:154-159)
-    double n = sqrt((r[0][0] * r[0][0] + i[0][0] * i[0][0]) + (r[0][1] * r[0][1] + i[0][1] * i[0][1]) +
+    T n = sqrt((r[0][0] * r[0][0] + i[0][0] * i[0][0]) + (r[0][1] * r[0][1] + i[0][1] * i[0][1]) +
                     (r[0][2] * r[0][2] + i[0][2] * i[0][2]));
     for (int c = 0; c < 3; ++c) {
         r[0][c] /= n;
         i[0][c] /= n;
     }
     // orthogonalise row 1 against row 0 (:108-118): w -= v * sum(conj(v) w)
-    double dr = 0.0, di = 0.0;
+    T dr = T(0), di = T(0);
     for (int c = 0; c < 3; ++c) {
         dr += r[0][c] * r[1][c] + i[0][c] * i[1][c];
         di += r[0][c] * i[1][c] - i[0][c] * r[1][c];
     }
     for (int c = 0; c < 3; ++c) {
-        const double pr = r[0][c] * dr - i[0][c] * di, pi = r[0][c] * di + i[0][c] * dr;
+        const T pr = r[0][c] * dr - i[0][c] * di, pi = r[0][c] * di + i[0][c] * dr;
         r[1][c] -= pr;
         i[1][c] -= pi;
     }
@@ -287,8 +289,8 @@ __device__ __forceinline__ void fix_su3_rows(double r[3][3], double i[3][3]) {
     // row 2 = conj(row0 x row1) (:120-135), normalised
     for (int c = 0; c < 3; ++c) {
         const int j = (c + 1) % 3, k = (c + 2) % 3;
-        const double re = (r[0][j] * r[1][k] - i[0][j] * i[1][k]) - (r[0][k] * r[1][j] - i[0][k] * i[1][j]);
-        const double im = (r[0][j] * i[1][k] + i[0][j] * r[1][k]) - (r[0][k] * i[1][j] + i[0][k] * r[1][j]);
+        const T re = (r[0][j] * r[1][k] - i[0][j] * i[1][k]) - (r[0][k] * r[1][j] - i[0][k] * i[1][j]);
+        const T im = (r[0][j] * i[1][k] + i[0][j] * r[1][k]) - (r[0][k] * i[1][j] + i[0][k] * r[1][j]);
         r[2][c] = re;
         i[2][c] = -im;
     }

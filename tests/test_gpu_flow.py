@@ -24,12 +24,14 @@ def _np_rk3(U, eps, nsteps):
     return W
 
 
-def test_rk3_step_matches_numpy():
+# eps 0.2: |X|_F reaches ~1, so the exponential's scale-and-square branch runs
+@pytest.mark.parametrize("eps,nsteps", [(0.02, 3), (0.2, 1)])
+def test_rk3_step_matches_numpy(eps, nsteps):
     U = generate.random_field((4, 4, 4, 4), 0.5, 3)
     f = GaugeField.from_array(U)
-    for _ in range(3):
-        flow.wflow_step(f, 0.02)
-    ref = _np_rk3(U, 0.02, 3)
+    for _ in range(nsteps):
+        flow.wflow_step(f, eps)
+    ref = _np_rk3(U, eps, nsteps)
     assert np.abs(f.to_numpy() - ref).max() < 1e-12
 
 
@@ -54,3 +56,14 @@ def test_flow_fp32_tracks_fp64():
     for a, b in zip(r64, r32):
         assert abs(a["plaq"] - b["plaq"]) < 1e-6
         assert abs(a["b2"] - b["b2"]) / a["b2"] < 1e-5
+
+
+def test_fp32_flow_no_drift():
+    """200 RK3 steps of 0.01 in FP32 (compensated reunitarisation) stay on the
+    FP64 trajectory: B^2 and the plaquette to ~1e-7 relative."""
+    U = generate.random_field((8, 8, 8, 8), 0.3, 6)
+    _, r64 = flow.wilson_flow(U, eps=0.01, tmax=2.0, measure_every=1.0)
+    _, r32 = flow.wilson_flow(GaugeField.from_array(U, prec="c64"), eps=0.01, tmax=2.0, measure_every=1.0)
+    for a, b in zip(r64, r32):
+        assert abs(a["b2"] - b["b2"]) / a["b2"] < 1e-6, (a, b)
+        assert abs(a["plaq"] - b["plaq"]) < 1e-7, (a, b)
