@@ -373,6 +373,14 @@ struct DevCache {
     int ncopy = 1;
     cudaStream_t cst[kCopyStreams] = {};
     cudaEvent_t cev[kCopyStreams + 1] = {};
+    // T-slab pipeline of the host-buffer B^2 force (created on first use):
+    // high-priority streams that stream slabs in (pack) and gradients out
+    // beside the compute on `st`, two buffer slots (packed slab + workspace)
+    bool pipe_init = false;
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t ev_go = nullptr, ev_in[2] = {}, ev_cp[2] = {}, ev_out[2] = {};
+    void* slot[2] = {};
+    size_t slot_bytes[2] = {};
 };
 
 // A device-usable address of host memory `p`, or NULL: pinned (page-locked,
@@ -508,6 +516,121 @@ double elapsed_s(DevCache* c) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->e0, c->e1);
     return (double)ms * 1e-3;
+}
+
+// Host-buffer B^2 and gradient, pipelined over time slabs.  B^2 uses only
+// spatial planes, so time slices are independent: slab k (nts time slices)
+// is packed from host memory on s_in, computed (lines, forward, line
+// cotangents) on st, and its link cotangents are written into the host
+// gradient on s_out, while slab k+1 is packed and slab k-1 written out.
+// The two I/O streams have the highest priority and capped grids, so they
+// take a few SMs and the host link (NVLink-C2C) while compute keeps the rest.
+// Per-slab B^2 partials are added on the host in slab order (deterministic).
+int pipe_setup(DevCache* c) {
+    if (c->pipe_init) return FLUE_OK;
+    int lo = 0, hi = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->s_in, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->s_out, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_go, cudaEventDisableTiming);
+    for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+        e = cudaEventCreateWithFlags(&c->ev_in[j], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_cp[j], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out[j], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+    c->pipe_init = true;
+    return FLUE_OK;
+}
+
+int env_int(const char* name, int dflt) {
+    const char* v = getenv(name);
+    return v ? atoi(v) : dflt;
+}
+
+// Number of time slabs for the pipelined host-buffer B^2 force: FLUE_SLABS,
+// else slabs of at least 8 time slices and 2^17 sites, at most 16 slabs;
+// 1 = no pipelining.
+int pipe_slabs(int NT, int64_t V) {
+    int s = env_int("FLUE_SLABS", 0);
+    if (s <= 0) {
+        const int64_t v3 = V / NT;
+        int nts = 8;
+        while ((int64_t)nts * v3 < ((int64_t)1 << 17) && nts < NT) nts *= 2;
+        s = (NT + nts - 1) / nts;
+        if (s > 16) s = 16;
+    }
+    if (s > NT) s = NT;
+    if (s > 32) s = 32;  // per-slab partials live in the 64-double scalar buffer
+    return s < 1 ? 1 : s;
+}
+
+int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int NT, int NX, int NY, int NZ, int prec,
+                             int form, double* B, void* d_grad, int nslab) {
+    int rc = pipe_setup(c);
+    if (rc) return rc;
+    const int64_t V = (int64_t)NT * NX * NY * NZ;
+    const int64_t st[7] = {1, NT, (int64_t)NT * NX, (int64_t)NT * NX * NY, V, 4 * V, 12 * V};
+    const int nts = (NT + nslab - 1) / nslab;
+    nslab = (NT + nts - 1) / nts;
+    const PlaneSet ps = b2_planes();
+    const Geom g0 = make_geom(nts, NX, NY, NZ);
+    const size_t fbytes = ((size_t)flue_field_bytes(nts, NX, NY, NZ, prec) + 255) & ~(size_t)255;
+    const size_t wbytes = energy_ws_bytes(g0, prec, ps, d_grad != nullptr);
+    for (int j = 0; j < 2; ++j)
+        if ((rc = grow(&c->slot[j], &c->slot_bytes[j], fbytes + wbytes))) return rc;
+    // grid caps of the I/O kernels (FLUE_IN_BLOCKS, FLUE_OUT_BLOCKS): measured
+    // on GB300 at 64x32^3, 8 slabs: 32 pack blocks of 256 threads and 16 x 4
+    // output blocks of 128 give 12.4 ms per call against 16.9 ms unpipelined;
+    // uncapped I/O grids take every SM and serialise with compute (16.9 ms),
+    // 8 / 4 starve the host link (22 ms)
+    const unsigned in_blocks = (unsigned)env_int("FLUE_IN_BLOCKS", 32);
+    const unsigned out_blocks = (unsigned)env_int("FLUE_OUT_BLOCKS", 16);
+    const size_t esz = data_dtype == FLUE_C128 ? 16 : 8;
+    cudaError_t e = cudaEventRecord(c->ev_go, c->st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_in, c->ev_go, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_out, c->ev_go, 0);
+    for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
+        const int j = k & 1, t0 = k * nts, n = NT - t0 < nts ? NT - t0 : nts;
+        const Geom g = make_geom(n, NX, NY, NZ);
+        char* buf = (char*)c->slot[j];
+        const FieldRef U{buf, g, prec};
+        // pack slab k once the compute of slab k-2 has read this slot
+        if (k >= 2 && (e = cudaStreamWaitEvent(c->s_in, c->ev_cp[j], 0)) != cudaSuccess) break;
+        if ((e = launch_pack((const char*)d_in + (size_t)t0 * esz, data_dtype, st, g, buf, prec, 0, c->s_in,
+                             in_blocks)) != cudaSuccess)
+            break;
+        if ((e = cudaEventRecord(c->ev_in[j], c->s_in)) != cudaSuccess) break;
+        // compute slab k once it is packed and the output of slab k-2 has
+        // left this slot's workspace
+        if ((e = cudaStreamWaitEvent(c->st, c->ev_in[j], 0)) != cudaSuccess) break;
+        if (k >= 2 && d_grad && (e = cudaStreamWaitEvent(c->st, c->ev_out[j], 0)) != cudaSuccess) break;
+        if ((e = launch_energy_slab_fwd(U, ps, V, c->scal + k, d_grad != nullptr, buf + fbytes, wbytes, c->st)) !=
+            cudaSuccess)
+            break;
+        if ((e = cudaEventRecord(c->ev_cp[j], c->st)) != cudaSuccess) break;
+        if (!d_grad) continue;
+        if ((e = cudaStreamWaitEvent(c->s_out, c->ev_cp[j], 0)) != cudaSuccess) break;
+        if ((e = launch_energy_slab_out(U, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, out_blocks, c->s_out)) !=
+            cudaSuccess)
+            break;
+        if ((e = cudaEventRecord(c->ev_out[j], c->s_out)) != cudaSuccess) break;
+    }
+    // everything joins st before the partials are read
+    for (int j = 0; j < 2 && e == cudaSuccess && d_grad; ++j)
+        if (j < nslab) e = cudaStreamWaitEvent(c->st, c->ev_out[j], 0);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(c->s_in);
+        cudaStreamSynchronize(c->s_out);
+        cudaStreamSynchronize(c->st);
+        return cuda_status(e);
+    }
+    double part[32];
+    if ((rc = fetch(c, part, c->scal, sizeof(double) * nslab))) return rc;
+    double b = 0.0;
+    for (int k = 0; k < nslab; ++k) b += part[k];
+    *B = b;
+    return FLUE_OK;
 }
 
 }  // namespace
@@ -721,6 +844,11 @@ int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int 
     // staging copies.  Otherwise the field is copied in and the gradient out.
     const void* d_in = device_view(data);
     void* d_grad = grad ? const_cast<void*>(device_view(grad)) : nullptr;
+    if (d_in && (!grad || d_grad)) {
+        const int nslab = pipe_slabs(NT, V);
+        if (nslab > 1)
+            return magnetic_force_pipelined(c, d_in, data_dtype, NT, NX, NY, NZ, prec, force_form, B, d_grad, nslab);
+    }
     flue_field U = {nullptr, NT, NX, NY, NZ, prec};
     if (d_in) {
         const size_t fb = (size_t)flue_field_bytes(NT, NX, NY, NZ, prec);
@@ -767,6 +895,11 @@ void flue_release_host_cache(void) {
         if (c->out) cudaFree(c->out);
         c->field = c->field2 = c->ws = c->out = nullptr;
         c->field_bytes = c->field2_bytes = c->ws_bytes = c->out_bytes = 0;
+        for (int j = 0; j < 2; ++j) {
+            if (c->slot[j]) cudaFree(c->slot[j]);
+            c->slot[j] = nullptr;
+            c->slot_bytes[j] = 0;
+        }
     }
 }
 

@@ -655,8 +655,13 @@ struct RefOut {
     C2* __restrict__ p;
     int64_t V;
     int nslot;
+    // T-slab output (nts > 0): site s of a sub-lattice with nts time slices
+    // goes to site t0 + s % nts + ntf * (s / nts) of the full lattice, whose
+    // time extent is ntf and volume V.  nts = 0: site s is site s.
+    int nts = 0, ntf = 0, t0 = 0;
     __device__ __forceinline__ void store(int64_t s, int slot, const M3<T>& m) const {
-        C2* q = p + s + V * slot;
+        const int64_t sf = nts ? (int64_t)t0 + s % nts + (int64_t)ntf * (s / nts) : s;
+        C2* q = p + sf + V * slot;
         const int64_t st = V * nslot;
 #pragma unroll
         for (int a = 0; a < 3; ++a)

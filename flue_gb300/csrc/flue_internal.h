@@ -21,8 +21,9 @@ cudaError_t launch_finish_sums(const double* partial, int nparts, int nout, doub
                                double scale = 1.0);
 
 // layouts
+// max_blocks > 0 caps the grid (the kernel is grid-strided)
 cudaError_t launch_pack(const void* src, int src_dtype, const int64_t strides[7], const Geom& g, void* dst, int dst_prec,
-                        int reunitarise, cudaStream_t st);
+                        int reunitarise, cudaStream_t st, unsigned max_blocks = 0);
 cudaError_t launch_unpack(const FieldRef& U, void* dst, int dst_dtype, cudaStream_t st);
 cudaError_t launch_matmul_batch(const void* l, const void* r, void* o, int64_t n, int dtype, int dagger, cudaStream_t st);
 cudaError_t launch_fix_field(void* links, const Geom& g, int prec, cudaStream_t st);
@@ -50,6 +51,17 @@ cudaError_t launch_fmunu(const FieldRef& U, int kind, int mu, int nu, void* out,
                          cudaStream_t st);
 cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int force_form, void* ws,
                           size_t ws_bytes, cudaStream_t st);
+// T-slab form of launch_energy for plane sets without the time direction
+// (B^2), where time slices are independent: U is a sub-lattice of the time
+// slices [t0, t0 + U.g.n[0]) of a lattice with time extent ntf and volume
+// vfull.  Part 1 (lines, forward, *out_E normalised by vfull, line
+// cotangents when with_force) and part 2 (link cotangents into the
+// full-lattice gradient, grid capped at max_blocks per direction when > 0)
+// use the same workspace and may run on different streams.
+cudaError_t launch_energy_slab_fwd(const FieldRef& U, const PlaneSet& ps, int64_t vfull, double* out_E, bool with_force,
+                                   void* ws, size_t ws_bytes, cudaStream_t st);
+cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
+                                   int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st);
 int plaqforce_blocks(const Geom& g);
 cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_S, void* force, int force_form,
                                    cudaStream_t st);

@@ -427,44 +427,46 @@ __global__ void __launch_bounds__(COT_BS, MinBlocks<T>::cot)
 }
 
 // ---------------------------------------------------------------------------
-// 4. link cotangents and gradient output: one thread per (site, direction)
+// 4. link cotangents and gradient output: one thread per (site, direction),
+//    grid-strided so that a capped grid can write the gradient to host memory
+//    beside other kernels
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void k_linkcot(Geom g, PlaneArg pa, MatAoS<T> lines, MatAoS<T> lam, T scale, int form, RefOut<T> out) {
-    const int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (z >= g.V) return;
     const int d = blockIdx.y;
     const int slot = sel(pa.slot, d);
-    if (slot < 0) {
-        out.store(z, d, m_zero<T>());
-        return;
-    }
-    int c[4];
-    site_coords(g, z, c);
-    int cd = 0, nd = 1;
-    int64_t sd = 1;
+    for (int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; z < g.V; z += (int64_t)gridDim.x * blockDim.x) {
+        if (slot < 0) {
+            out.store(z, d, m_zero<T>());
+            continue;
+        }
+        int c[4];
+        site_coords(g, z, c);
+        int cd = 0, nd = 1;
+        int64_t sd = 1;
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
-    const int64_t zp = z + (int64_t)wrapd(cd, 1, nd) * sd, zm = z + (int64_t)wrapd(cd, -1, nd) * sd,
-                  zmm = z + (int64_t)wrapd(cd, -2, nd) * sd;
-    const int l1 = 3 * slot, l2 = 3 * slot + 1;
-    const M3<T> up = lines.load(zp, l1);
-    const M3<T> um = lines.load(zm, l1);
-    M3<T> n = lam.load(z, 3 * slot);
-    mac<false, false>(n, up, lam.load(z, 3 * slot + 1));
-    mac<false, false>(n, lam.load(zm, 3 * slot + 1), um);
-    mac<false, false>(n, lines.load(zp, l2), lam.load(z, 3 * slot + 2));
-    {
-        const M3<T> t = mul(up, lam.load(zm, 3 * slot + 2));
-        mac<false, false>(n, t, um);
-    }
-    mac<false, false>(n, lam.load(zmm, 3 * slot + 2), lines.load(zmm, l2));
-    if (form == 0) {
-        const M3<T> un = mul(lines.load(z, l1), n);
-        out.store(z, d, ta_scaled(un, T(-0.5) * scale));
-    } else {
-        out.store(z, d, m_scale(dag(n), scale));
+        for (int k = 0; k < 4; ++k)
+            if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
+        const int64_t zp = z + (int64_t)wrapd(cd, 1, nd) * sd, zm = z + (int64_t)wrapd(cd, -1, nd) * sd,
+                      zmm = z + (int64_t)wrapd(cd, -2, nd) * sd;
+        const int l1 = 3 * slot, l2 = 3 * slot + 1;
+        const M3<T> up = lines.load(zp, l1);
+        const M3<T> um = lines.load(zm, l1);
+        M3<T> n = lam.load(z, 3 * slot);
+        mac<false, false>(n, up, lam.load(z, 3 * slot + 1));
+        mac<false, false>(n, lam.load(zm, 3 * slot + 1), um);
+        mac<false, false>(n, lines.load(zp, l2), lam.load(z, 3 * slot + 2));
+        {
+            const M3<T> t = mul(up, lam.load(zm, 3 * slot + 2));
+            mac<false, false>(n, t, um);
+        }
+        mac<false, false>(n, lam.load(zmm, 3 * slot + 2), lines.load(zmm, l2));
+        if (form == 0) {
+            const M3<T> un = mul(lines.load(z, l1), n);
+            out.store(z, d, ta_scaled(un, T(-0.5) * scale));
+        } else {
+            out.store(z, d, m_scale(dag(n), scale));
+        }
     }
 }
 
@@ -554,12 +556,14 @@ static inline void stage_mark(int k, cudaStream_t st) {
     }
 }
 
+// Part 1 of the pipeline: lines, forward (+ energy sum normalised by vnorm),
+// line cotangents when `with_force`.
 template <class L, typename T>
-static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, int kind, double* out_E, void* force,
-                               int form, char* ws, const EnergyWs& w, RefOut<T> fout, cudaStream_t st) {
-    using C2 = typename V2<T>::type;
+static cudaError_t energy_fwd_part(const L& U, const Geom& g, const PlaneArg& pa, int kind, double* out_E,
+                                   bool with_force, double vnorm, char* ws, const EnergyWs& w, RefOut<T> fout,
+                                   cudaStream_t st) {
     MatAoS<T> lines{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lines), g.V};
-    AHAoS<T> kb{force ? reinterpret_cast<decltype(AHAoS<T>::p)>(ws + w.kbuf) : nullptr, g.V};
+    AHAoS<T> kb{with_force ? reinterpret_cast<decltype(AHAoS<T>::p)>(ws + w.kbuf) : nullptr, g.V};
     MatAoS<T> lam{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lam), g.V};
     double* part = out_E ? (double*)(ws + w.part) : nullptr;
     const unsigned nbx = (unsigned)((g.V + FWD_BS - 1) / FWD_BS);
@@ -570,19 +574,39 @@ static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, in
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (out_E) {
-        e = launch_finish_sums(part, (int)(nbx * pa.np), 1, out_E, st, 1.0 / (double)g.V);
+        e = launch_finish_sums(part, (int)(nbx * pa.np), 1, out_E, st, 1.0 / vnorm);
         if (e != cudaSuccess) return e;
     }
     stage_mark(2, st);
-    if (!force) return cudaSuccess;
+    if (!with_force) return cudaSuccess;
     const unsigned nbc = (unsigned)((g.V + COT_BS - 1) / COT_BS);
     k_linecot<T><<<nbc * 3 * pa.nd, COT_BS, 0, st>>>(g, pa, lines, kb, lam);
     stage_mark(3, st);
-    RefOut<T> fo{(C2*)force, g.V, 4};
-    const T scale = (T)(-1.0 / (2.0 * (double)g.V));
-    k_linkcot<T><<<dim3((unsigned)((g.V + 127) / 128), 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo);
+    return cudaGetLastError();
+}
+
+// Part 2: link cotangents, gradient of E/vnorm written through `fo`.
+template <typename T>
+static cudaError_t energy_out_part(const Geom& g, const PlaneArg& pa, double vnorm, int form, char* ws,
+                                   const EnergyWs& w, RefOut<T> fo, unsigned max_blocks, cudaStream_t st) {
+    MatAoS<T> lines{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lines), g.V};
+    MatAoS<T> lam{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lam), g.V};
+    const T scale = (T)(-1.0 / (2.0 * vnorm));
+    unsigned nb = (unsigned)((g.V + 127) / 128);
+    if (max_blocks && nb > max_blocks) nb = max_blocks;
+    k_linkcot<T><<<dim3(nb, 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo);
     stage_mark(4, st);
     return cudaGetLastError();
+}
+
+template <class L, typename T>
+static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, int kind, double* out_E, void* force,
+                               int form, char* ws, const EnergyWs& w, RefOut<T> fout, cudaStream_t st) {
+    using C2 = typename V2<T>::type;
+    cudaError_t e = energy_fwd_part<L, T>(U, g, pa, kind, out_E, force != nullptr, (double)g.V, ws, w, fout, st);
+    if (e != cudaSuccess || !force) return e;
+    RefOut<T> fo{(C2*)force, g.V, 4};
+    return energy_out_part<T>(g, pa, (double)g.V, form, ws, w, fo, 0, st);
 }
 
 cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int force_form, void* ws,
@@ -595,6 +619,40 @@ cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, 
         return energy_impl<decltype(L), T>(L, U.g, pa, 1, out_E, force, force_form, (char*)ws, w, none, st);
     });
     return cudaSuccess;
+}
+
+static bool has_time_plane(const PlaneSet& ps) {
+    for (int p = 0; p < ps.np; ++p)
+        if (ps.mu[p] == 0 || ps.nu[p] == 0) return true;
+    return false;
+}
+
+cudaError_t launch_energy_slab_fwd(const FieldRef& U, const PlaneSet& ps, int64_t vfull, double* out_E, bool with_force,
+                                   void* ws, size_t ws_bytes, cudaStream_t st) {
+    if (has_time_plane(ps) || vfull < U.g.V) return cudaErrorInvalidValue;
+    const PlaneArg pa = make_planes(ps);
+    const EnergyWs w = energy_layout(U.g, U.prec, pa, with_force);
+    if (ws_bytes < w.total) return cudaErrorInvalidValue;
+    FLUE_DISPATCH_LINKS(U, {
+        RefOut<T> none{nullptr, U.g.V, 1};
+        return energy_fwd_part<decltype(L), T>(L, U.g, pa, 1, out_E, with_force, (double)vfull, (char*)ws, w, none,
+                                               st);
+    });
+    return cudaSuccess;
+}
+
+cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
+                                   int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st) {
+    if (has_time_plane(ps) || vfull < U.g.V || t0 < 0 || t0 + U.g.n[0] > ntf) return cudaErrorInvalidValue;
+    const PlaneArg pa = make_planes(ps);
+    const EnergyWs w = energy_layout(U.g, U.prec, pa, true);
+    if (ws_bytes < w.total) return cudaErrorInvalidValue;
+    if (U.prec == PREC_C128) {
+        RefOut<double> fo{(double2*)force, vfull, 4, U.g.n[0], ntf, t0};
+        return energy_out_part<double>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
+    }
+    RefOut<float> fo{(float2*)force, vfull, 4, U.g.n[0], ntf, t0};
+    return energy_out_part<float>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
 }
 
 // F_munu of one plane: kind 0 = clover (cloverLoopMuNuCoord), 1 = 5-loop

@@ -57,16 +57,16 @@ cudaError_t launch_finish_sums(const double* partial, int nparts, int nout, doub
 
 // ---------------------------------------------------------------------------
 // pack: arbitrary-strided (t,x,y,z,mu,a,b) complex128/complex64 -> device
-// layout, optionally reunitarised.  One thread per (site, mu).
+// layout, optionally reunitarised.  One thread per (site, mu), grid-strided
+// so that a capped grid can stream a field in beside other kernels.
 // ---------------------------------------------------------------------------
 struct Strides7 {
     int64_t s[7];
 };
 
 template <typename SRC>
-__global__ void k_pack(const SRC* __restrict__ src, Strides7 sd, Geom g, void* __restrict__ dst, int dst_prec, int reun) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= 4 * g.V) return;
+__device__ __forceinline__ void pack_one(const SRC* __restrict__ src, const Strides7& sd, const Geom& g,
+                                         void* __restrict__ dst, int dst_prec, int reun, int64_t idx) {
     const int64_t s = idx % g.V;
     const int mu = (int)(idx / g.V);
     int c[4];
@@ -96,13 +96,21 @@ __global__ void k_pack(const SRC* __restrict__ src, Strides7 sd, Geom g, void* _
     }
 }
 
+template <typename SRC>
+__global__ void k_pack(const SRC* __restrict__ src, Strides7 sd, Geom g, void* __restrict__ dst, int dst_prec, int reun) {
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < 4 * g.V;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        pack_one(src, sd, g, dst, dst_prec, reun, idx);
+}
+
 cudaError_t launch_pack(const void* src, int src_dtype, const int64_t strides[7], const Geom& g, void* dst, int dst_prec,
-                        int reunitarise, cudaStream_t st) {
+                        int reunitarise, cudaStream_t st, unsigned max_blocks) {
     Strides7 sd;
     for (int k = 0; k < 7; ++k) sd.s[k] = strides[k];
     const int64_t n = 4 * g.V;
     const int bs = 256;
-    const unsigned nb = (unsigned)((n + bs - 1) / bs);
+    unsigned nb = (unsigned)((n + bs - 1) / bs);
+    if (max_blocks && nb > max_blocks) nb = max_blocks;
     if (src_dtype == PREC_C128)
         k_pack<double2><<<nb, bs, 0, st>>>((const double2*)src, sd, g, dst, dst_prec, reunitarise);
     else
