@@ -7,6 +7,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -114,6 +115,29 @@ int check_ws(int op, const FieldRef& F, size_t ws_bytes, const void* ws) {
     return FLUE_OK;
 }
 
+// Time slabs of a device energy evaluation whose planes leave out the time
+// direction (B^2): FLUE_SLABS slabs, else slabs of at least 2^17 sites (at
+// most 16), on FLUE_SLAB_STREAMS streams (default 4).  Measured on GB300,
+// B^2 force at 64x32^3 FP32: one pass 11.5 ms, 16 slabs on 4 streams 10.6 ms.
+int device_slabs(const Geom& g, const PlaneSet& ps, int* nstream) {
+    for (int p = 0; p < ps.np; ++p)
+        if (ps.mu[p] == 0 || ps.nu[p] == 0) return 1;
+    const char* env = getenv("FLUE_SLABS");
+    int n = env ? atoi(env) : 0;
+    if (n <= 0) {
+        const int64_t v3 = g.V / g.n[0];
+        int nts = 1;
+        while ((int64_t)nts * v3 < ((int64_t)1 << 17) && nts < g.n[0]) nts *= 2;
+        n = (g.n[0] + nts - 1) / nts;
+        if (n > 16) n = 16;
+    }
+    if (n > g.n[0]) n = g.n[0];
+    const char* es = getenv("FLUE_SLAB_STREAMS");
+    int k = es ? atoi(es) : 4;
+    *nstream = k < 1 ? 1 : (k > 4 ? 4 : k);
+    return n < 1 ? 1 : n;
+}
+
 int energy_common(const flue_field* U, const PlaneSet& ps, int op, double* d_E, void* d_force, int form, void* ws,
                   size_t ws_bytes, void* stream) {
     FieldRef F;
@@ -127,12 +151,22 @@ int energy_common(const flue_field* U, const PlaneSet& ps, int op, double* d_E, 
         return FLUE_ERR_WORKSPACE;
     }
     (void)op;
+    if (!stage_timing_on()) {
+        int nstream = 1;
+        const int nslab = device_slabs(F.g, ps, &nstream);
+        if (nslab > 1 && ws_bytes >= energy_slabs_ws_bytes(F.g, F.prec, ps, d_force != nullptr, nslab, nstream))
+            return cuda_status(
+                launch_energy_slabs(F, ps, d_E, d_force, form, ws, ws_bytes, nslab, nstream, (cudaStream_t)stream));
+    }
     return cuda_status(launch_energy(F, ps, d_E, d_force, form, ws, ws_bytes, (cudaStream_t)stream));
 }
 
 }  // namespace
 
 void flue::set_error_detail(const char* msg) { snprintf(g_detail, sizeof(g_detail), "%s", msg); }
+
+static std::atomic<unsigned long long> g_launches{0};
+void flue::note_launch(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 extern "C" {
 
@@ -168,6 +202,8 @@ const char* flue_last_error_detail(void) { return g_detail; }
 int flue_abi_version(void) { return 1; }
 
 int flue_stage_timing(int enable) { return cuda_status(stage_timing_enable(enable)); }
+
+uint64_t flue_kernel_launches(void) { return (uint64_t)g_launches.load(std::memory_order_relaxed); }
 
 int flue_stage_times(double* ms, int max_stages, int* n_stages) {
     if (!ms || !n_stages || max_stages < 0) return fail(FLUE_ERR_ARG, "NULL pointer");
@@ -605,8 +641,8 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
         // left this slot's workspace
         if ((e = cudaStreamWaitEvent(c->st, c->ev_in[j], 0)) != cudaSuccess) break;
         if (k >= 2 && d_grad && (e = cudaStreamWaitEvent(c->st, c->ev_out[j], 0)) != cudaSuccess) break;
-        if ((e = launch_energy_slab_fwd(U, ps, V, c->scal + k, d_grad != nullptr, buf + fbytes, wbytes, c->st)) !=
-            cudaSuccess)
+        if ((e = launch_energy_slab_fwd(U, 0, n, ps, V, c->scal + k, d_grad != nullptr, buf + fbytes, wbytes,
+                                        c->st)) != cudaSuccess)
             break;
         if ((e = cudaEventRecord(c->ev_cp[j], c->st)) != cudaSuccess) break;
         if (!d_grad) continue;

@@ -274,17 +274,17 @@ static cudaError_t ens_launch(flue_ensemble* e, double* d_out, cudaStream_t st) 
     cudaError_t r = cudaMemsetAsync(e->d_counter, 0, sizeof(int), st);
     if (r != cudaSuccess) return r;
     if (e->prec == PREC_C128)
-        k_ensemble<FullLinks<double>, double>
+        note_launch(), k_ensemble<FullLinks<double>, double>
             <<<e->grid, e->block, 0, st>>>(e->d_fields, e->d_items, e->nitems, e->d_counter, e->d_part, e->with_b2);
     else if (e->prec == PREC_C64)
-        k_ensemble<FullLinks<float>, float>
+        note_launch(), k_ensemble<FullLinks<float>, float>
             <<<e->grid, e->block, 0, st>>>(e->d_fields, e->d_items, e->nitems, e->d_counter, e->d_part, e->with_b2);
     else
-        k_ensemble<R12Links, float>
+        note_launch(), k_ensemble<R12Links, float>
             <<<e->grid, e->block, 0, st>>>(e->d_fields, e->d_items, e->nitems, e->d_counter, e->d_part, e->with_b2);
     r = cudaGetLastError();
     if (r != cudaSuccess) return r;
-    k_ensemble_finish<<<e->nfields, 32, 0, st>>>(e->d_part, e->d_first, e->d_fields, e->nfields, d_out);
+    note_launch(), k_ensemble_finish<<<e->nfields, 32, 0, st>>>(e->d_part, e->d_first, e->d_fields, e->nfields, d_out);
     return cudaGetLastError();
 }
 
@@ -396,6 +396,7 @@ int flue_ensemble_capture(flue_ensemble* e, double* d_out) {
 
 int flue_ensemble_replay(flue_ensemble* e, void* stream) {
     if (!e || !e->exec) return FLUE_ERR_ARG;
+    flue::note_launch(2);  // the graph holds the persistent kernel and its finisher
     return cudaGraphLaunch(e->exec, (cudaStream_t)stream) == cudaSuccess ? FLUE_OK : FLUE_ERR_CUDA;
 }
 

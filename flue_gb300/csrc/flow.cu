@@ -304,9 +304,9 @@ cudaError_t launch_wflow_step(void* links, const Geom& g, int prec, double eps, 
         cudaError_t e = launch_plaquette_force(U, part, nullptr, force, 0, st);
         if (e != cudaSuccess) return e;
         if (prec == PREC_C128)
-            k_wflow_update<double><<<nb, 128, 0, st>>>(links, g, force, bb, eps, stage, 0);
+            note_launch(), k_wflow_update<double><<<nb, 128, 0, st>>>(links, g, force, bb, eps, stage, 0);
         else
-            k_wflow_update<float><<<nb, 128, 0, st>>>(links, g, force, bbf, (float)eps, stage, 1);
+            note_launch(), k_wflow_update<float><<<nb, 128, 0, st>>>(links, g, force, bbf, (float)eps, stage, 1);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

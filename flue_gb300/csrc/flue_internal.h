@@ -52,22 +52,35 @@ cudaError_t launch_fmunu(const FieldRef& U, int kind, int mu, int nu, void* out,
 cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int force_form, void* ws,
                           size_t ws_bytes, cudaStream_t st);
 // T-slab form of launch_energy for plane sets without the time direction
-// (B^2), where time slices are independent: U is a sub-lattice of the time
-// slices [t0, t0 + U.g.n[0]) of a lattice with time extent ntf and volume
-// vfull.  Part 1 (lines, forward, *out_E normalised by vfull, line
-// cotangents when with_force) and part 2 (link cotangents into the
-// full-lattice gradient, grid capped at max_blocks per direction when > 0)
-// use the same workspace and may run on different streams.
-cudaError_t launch_energy_slab_fwd(const FieldRef& U, const PlaneSet& ps, int64_t vfull, double* out_E, bool with_force,
-                                   void* ws, size_t ws_bytes, cudaStream_t st);
+// (B^2), where time slices are independent.  Part 1 (lines, forward, *out_E
+// normalised by vfull, line cotangents when with_force) computes the slab of
+// time slices [t0, t0 + nts) of field U (the whole field, or a packed slab
+// with t0 = 0).  Part 2 (link cotangents into the full-lattice gradient of
+// time extent ntf, grid capped at max_blocks per direction when > 0) takes U
+// with the slab's geometry (links unused).  Both use the same workspace, sized
+// for the slab, and may run on different streams.
+cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const PlaneSet& ps, int64_t vfull,
+                                   double* out_E, bool with_force, void* ws, size_t ws_bytes, cudaStream_t st);
 cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
                                    int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st);
+// launch_energy over nslab time slabs on nstream (<= 4) streams forked from
+// st (plane sets without the time direction); workspace of
+// energy_slabs_ws_bytes(...) bytes.  Results equal launch_energy's: the
+// gradient bitwise, the energy up to the order of the FP64 partial sums.
+size_t energy_slabs_ws_bytes(const Geom& g, int prec, const PlaneSet& ps, bool with_force, int nslab, int nstream);
+cudaError_t launch_energy_slabs(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int form, void* ws,
+                                size_t ws_bytes, int nslab, int nstream, cudaStream_t st);
+bool stage_timing_on();
 int plaqforce_blocks(const Geom& g);
 cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_S, void* force, int force_form,
                                    cudaStream_t st);
 
 // text returned by flue_last_error_detail() on the calling thread
 void set_error_detail(const char* msg);
+
+// process-wide count of kernel launches (flue_kernel_launches); every launch
+// site calls it as `note_launch(), kernel<<<...>>>(...)`
+void note_launch(int n = 1);
 
 cudaError_t stage_timing_enable(int on);
 cudaError_t stage_times(double* ms, int maxn, int* n);

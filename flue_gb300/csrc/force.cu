@@ -30,6 +30,8 @@
 //   4. link cotangents N_d(z) from the line cotangents of the lines through
 //      the link, then the su(3)-projected gradient G = -1/2 TA(U N) or the
 //      Euclidean gradient N^+                              (k_linkcot)
+#include <mutex>
+
 #include "flue_internal.h"
 
 namespace flue {
@@ -198,10 +200,13 @@ __device__ __forceinline__ void corner_off(int k, int a, int b, int& di, int& dj
 
 // ---------------------------------------------------------------------------
 // 1. lines: L^1_d(y) = U_d(y) (expanded to 18 reals), L^2_d(y) = U_d(y) U_d(y+d),
-//    L^3_d(y) = L^2_d(y) U_d(y+2d)
+//    L^3_d(y) = L^2_d(y) U_d(y+2d).  Sites are those of geometry g; the links
+//    are read from a field of geometry gs at time offset t0 (gs = g, t0 = 0
+//    for a whole lattice; a time slab of a larger field otherwise -- the lines
+//    never step in time then).
 // ---------------------------------------------------------------------------
 template <class L, typename T>
-__global__ void k_lines(L U, Geom g, PlaneArg pa, MatAoS<T> lines) {
+__global__ void k_lines(L U, Geom g, Geom gs, int t0, PlaneArg pa, MatAoS<T> lines) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     const int slot = blockIdx.y;
@@ -212,10 +217,11 @@ __global__ void k_lines(L U, Geom g, PlaneArg pa, MatAoS<T> lines) {
     int64_t sd = 1;
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
-    const int64_t s1 = s + (int64_t)wrapd(cd, 1, nd) * sd;
-    const int64_t s2 = s + (int64_t)wrapd(cd, 2, nd) * sd;
-    const M3<T> u0 = U.load(s, d);
+        if (k == d) cd = c[k], nd = g.n[k], sd = gs.st[k];
+    const int64_t u = (int64_t)(t0 + c[0]) + c[1] * gs.st[1] + c[2] * gs.st[2] + c[3] * gs.st[3];
+    const int64_t s1 = u + (int64_t)wrapd(cd, 1, nd) * sd;
+    const int64_t s2 = u + (int64_t)wrapd(cd, 2, nd) * sd;
+    const M3<T> u0 = U.load(u, d);
     const M3<T> l2 = mul(u0, U.load(s1, d));
     lines.store(s, 3 * slot, u0);
     lines.store(s, 3 * slot + 1, l2);
@@ -559,18 +565,18 @@ static inline void stage_mark(int k, cudaStream_t st) {
 // Part 1 of the pipeline: lines, forward (+ energy sum normalised by vnorm),
 // line cotangents when `with_force`.
 template <class L, typename T>
-static cudaError_t energy_fwd_part(const L& U, const Geom& g, const PlaneArg& pa, int kind, double* out_E,
-                                   bool with_force, double vnorm, char* ws, const EnergyWs& w, RefOut<T> fout,
-                                   cudaStream_t st) {
+static cudaError_t energy_fwd_part(const L& U, const Geom& g, const Geom& gs, int t0, const PlaneArg& pa, int kind,
+                                   double* out_E, bool with_force, double vnorm, char* ws, const EnergyWs& w,
+                                   RefOut<T> fout, cudaStream_t st) {
     MatAoS<T> lines{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lines), g.V};
     AHAoS<T> kb{with_force ? reinterpret_cast<decltype(AHAoS<T>::p)>(ws + w.kbuf) : nullptr, g.V};
     MatAoS<T> lam{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lam), g.V};
     double* part = out_E ? (double*)(ws + w.part) : nullptr;
     const unsigned nbx = (unsigned)((g.V + FWD_BS - 1) / FWD_BS);
     stage_mark(0, st);
-    k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, pa, lines);
+    note_launch(), k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, gs, t0, pa, lines);
     stage_mark(1, st);
-    k_fwd<T><<<nbx * pa.np, FWD_BS, 0, st>>>(g, pa, kind, lines, kb, fout, part);
+    note_launch(), k_fwd<T><<<nbx * pa.np, FWD_BS, 0, st>>>(g, pa, kind, lines, kb, fout, part);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (out_E) {
@@ -580,7 +586,7 @@ static cudaError_t energy_fwd_part(const L& U, const Geom& g, const PlaneArg& pa
     stage_mark(2, st);
     if (!with_force) return cudaSuccess;
     const unsigned nbc = (unsigned)((g.V + COT_BS - 1) / COT_BS);
-    k_linecot<T><<<nbc * 3 * pa.nd, COT_BS, 0, st>>>(g, pa, lines, kb, lam);
+    note_launch(), k_linecot<T><<<nbc * 3 * pa.nd, COT_BS, 0, st>>>(g, pa, lines, kb, lam);
     stage_mark(3, st);
     return cudaGetLastError();
 }
@@ -594,7 +600,7 @@ static cudaError_t energy_out_part(const Geom& g, const PlaneArg& pa, double vno
     const T scale = (T)(-1.0 / (2.0 * vnorm));
     unsigned nb = (unsigned)((g.V + 127) / 128);
     if (max_blocks && nb > max_blocks) nb = max_blocks;
-    k_linkcot<T><<<dim3(nb, 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo);
+    note_launch(), k_linkcot<T><<<dim3(nb, 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo);
     stage_mark(4, st);
     return cudaGetLastError();
 }
@@ -603,7 +609,8 @@ template <class L, typename T>
 static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, int kind, double* out_E, void* force,
                                int form, char* ws, const EnergyWs& w, RefOut<T> fout, cudaStream_t st) {
     using C2 = typename V2<T>::type;
-    cudaError_t e = energy_fwd_part<L, T>(U, g, pa, kind, out_E, force != nullptr, (double)g.V, ws, w, fout, st);
+    cudaError_t e =
+        energy_fwd_part<L, T>(U, g, g, 0, pa, kind, out_E, force != nullptr, (double)g.V, ws, w, fout, st);
     if (e != cudaSuccess || !force) return e;
     RefOut<T> fo{(C2*)force, g.V, 4};
     return energy_out_part<T>(g, pa, (double)g.V, form, ws, w, fo, 0, st);
@@ -627,16 +634,18 @@ static bool has_time_plane(const PlaneSet& ps) {
     return false;
 }
 
-cudaError_t launch_energy_slab_fwd(const FieldRef& U, const PlaneSet& ps, int64_t vfull, double* out_E, bool with_force,
-                                   void* ws, size_t ws_bytes, cudaStream_t st) {
-    if (has_time_plane(ps) || vfull < U.g.V) return cudaErrorInvalidValue;
+cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const PlaneSet& ps, int64_t vfull,
+                                   double* out_E, bool with_force, void* ws, size_t ws_bytes, cudaStream_t st) {
+    if (has_time_plane(ps) || t0 < 0 || nts < 1 || t0 + nts > U.g.n[0]) return cudaErrorInvalidValue;
+    const Geom g = make_geom(nts, U.g.n[1], U.g.n[2], U.g.n[3]);
+    if (vfull < g.V) return cudaErrorInvalidValue;
     const PlaneArg pa = make_planes(ps);
-    const EnergyWs w = energy_layout(U.g, U.prec, pa, with_force);
+    const EnergyWs w = energy_layout(g, U.prec, pa, with_force);
     if (ws_bytes < w.total) return cudaErrorInvalidValue;
     FLUE_DISPATCH_LINKS(U, {
-        RefOut<T> none{nullptr, U.g.V, 1};
-        return energy_fwd_part<decltype(L), T>(L, U.g, pa, 1, out_E, with_force, (double)vfull, (char*)ws, w, none,
-                                               st);
+        RefOut<T> none{nullptr, g.V, 1};
+        return energy_fwd_part<decltype(L), T>(L, g, U.g, t0, pa, 1, out_E, with_force, (double)vfull, (char*)ws, w,
+                                               none, st);
     });
     return cudaSuccess;
 }
@@ -653,6 +662,107 @@ cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_
     }
     RefOut<float> fo{(float2*)force, vfull, 4, U.g.n[0], ntf, t0};
     return energy_out_part<float>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
+}
+
+// ---------------------------------------------------------------------------
+// Energy (and gradient) of a device field over time slabs on several streams.
+// Plane sets without the time direction (B^2) leave time slices independent,
+// so the field is processed as nslab slabs of consecutive time slices, slab
+// k on stream k % nstream (the caller's stream and nstream - 1 library
+// streams, forked from and joined back to the caller's stream by events).
+// The memory-bound stages (lines, link cotangents) of one slab then overlap
+// the compute-bound ones of another, and each slab's intermediates are 1/nslab
+// of the lattice's.  Per-slab energies are added in slab order by one
+// finisher; the gradient is written in place through the slab mapping, so
+// both are bitwise independent of the stream schedule.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kMaxSlabStreams = 4;
+struct SlabStreams {
+    std::mutex m;
+    cudaStream_t s[kMaxSlabStreams - 1] = {};
+    cudaEvent_t fork = nullptr, join[kMaxSlabStreams - 1] = {};
+};
+std::mutex g_slab_mtx;
+SlabStreams* g_slab[64] = {};
+
+cudaError_t slab_streams(SlabStreams** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_slab_mtx);
+    if (!g_slab[dev]) {
+        SlabStreams* ss = new SlabStreams();
+        for (int i = 0; i < kMaxSlabStreams - 1 && e == cudaSuccess; ++i) {
+            e = cudaStreamCreateWithFlags(&ss->s[i], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ss->join[i], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ss->fork, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;  // (a failed setup keeps its handles; it is retried on the next call)
+        g_slab[dev] = ss;
+    }
+    *out = g_slab[dev];
+    return cudaSuccess;
+}
+
+struct SlabWs {
+    size_t slot, spart, total;
+};
+SlabWs slab_ws_layout(const Geom& g, int prec, const PlaneArg& pa, bool with_force, int nslab, int nstream) {
+    const int nts = (g.n[0] + nslab - 1) / nslab;
+    const Geom gs = make_geom(nts, g.n[1], g.n[2], g.n[3]);
+    SlabWs w;
+    w.slot = energy_layout(gs, prec, pa, with_force).total;
+    w.spart = (size_t)nstream * w.slot;
+    w.total = align256(w.spart + (size_t)nslab * sizeof(double));
+    return w;
+}
+}  // namespace
+
+bool stage_timing_on() { return g_stage_on; }
+
+size_t energy_slabs_ws_bytes(const Geom& g, int prec, const PlaneSet& ps, bool with_force, int nslab, int nstream) {
+    return slab_ws_layout(g, prec, make_planes(ps), with_force, nslab, nstream).total;
+}
+
+cudaError_t launch_energy_slabs(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int form, void* ws,
+                                size_t ws_bytes, int nslab, int nstream, cudaStream_t st) {
+    if (has_time_plane(ps) || nslab < 1 || nslab > U.g.n[0] || nstream < 1 || nstream > kMaxSlabStreams)
+        return cudaErrorInvalidValue;
+    const PlaneArg pa = make_planes(ps);
+    const bool with_force = force != nullptr;
+    const SlabWs w = slab_ws_layout(U.g, U.prec, pa, with_force, nslab, nstream);
+    if (ws_bytes < w.total) return cudaErrorInvalidValue;
+    const int nts = (U.g.n[0] + nslab - 1) / nslab;
+    nslab = (U.g.n[0] + nts - 1) / nts;
+    if (nstream > nslab) nstream = nslab;
+    SlabStreams* ss = nullptr;
+    cudaError_t e = slab_streams(&ss);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(ss->m);
+    double* spart = out_E ? (double*)((char*)ws + w.spart) : nullptr;
+    if ((e = cudaEventRecord(ss->fork, st)) != cudaSuccess) return e;
+    for (int i = 1; i < nstream; ++i)
+        if ((e = cudaStreamWaitEvent(ss->s[i - 1], ss->fork, 0)) != cudaSuccess) return e;
+    for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
+        const int i = k % nstream, t0 = k * nts, n = U.g.n[0] - t0 < nts ? U.g.n[0] - t0 : nts;
+        cudaStream_t sk = i == 0 ? st : ss->s[i - 1];
+        char* slot = (char*)ws + (size_t)i * w.slot;
+        e = launch_energy_slab_fwd(U, t0, n, ps, U.g.V, spart ? spart + k : nullptr, with_force, slot, w.slot, sk);
+        if (e == cudaSuccess && with_force) {
+            const FieldRef Us{U.links, make_geom(n, U.g.n[1], U.g.n[2], U.g.n[3]), U.prec};
+            e = launch_energy_slab_out(Us, ps, U.g.V, U.g.n[0], t0, force, form, slot, w.slot, 0, sk);
+        }
+    }
+    // join every library stream back into the caller's stream, also on error
+    for (int i = 1; i < nstream; ++i) {
+        cudaError_t r = cudaEventRecord(ss->join[i - 1], ss->s[i - 1]);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(st, ss->join[i - 1], 0);
+        if (e == cudaSuccess) e = r;
+    }
+    if (e == cudaSuccess && out_E) e = launch_finish_sums(spart, nslab, 1, out_E, st, 1.0);
+    return e;
 }
 
 // F_munu of one plane: kind 0 = clover (cloverLoopMuNuCoord), 1 = 5-loop
@@ -725,7 +835,7 @@ cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_
     FLUE_DISPATCH_LINKS(U, {
         using C2 = typename V2<T>::type;
         RefOut<T> fo{(C2*)force, U.g.V, 4};
-        k_plaqforce<decltype(L), T><<<dim3(nb, 4), PF_BS, 0, st>>>(L, U.g, force_form, fo, out_S ? part : nullptr);
+        note_launch(), k_plaqforce<decltype(L), T><<<dim3(nb, 4), PF_BS, 0, st>>>(L, U.g, force_form, fo, out_S ? part : nullptr);
     });
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !out_S) return e;

@@ -51,7 +51,7 @@ __global__ void k_finish_sums(const double* __restrict__ part, int nparts, doubl
 }
 
 cudaError_t launch_finish_sums(const double* partial, int nparts, int nout, double* out, cudaStream_t st, double scale) {
-    k_finish_sums<<<nout, 256, 0, st>>>(partial, nparts, scale, out);
+    note_launch(), k_finish_sums<<<nout, 256, 0, st>>>(partial, nparts, scale, out);
     return cudaGetLastError();
 }
 
@@ -112,9 +112,9 @@ cudaError_t launch_pack(const void* src, int src_dtype, const int64_t strides[7]
     unsigned nb = (unsigned)((n + bs - 1) / bs);
     if (max_blocks && nb > max_blocks) nb = max_blocks;
     if (src_dtype == PREC_C128)
-        k_pack<double2><<<nb, bs, 0, st>>>((const double2*)src, sd, g, dst, dst_prec, reunitarise);
+        note_launch(), k_pack<double2><<<nb, bs, 0, st>>>((const double2*)src, sd, g, dst, dst_prec, reunitarise);
     else
-        k_pack<float2><<<nb, bs, 0, st>>>((const float2*)src, sd, g, dst, dst_prec, reunitarise);
+        note_launch(), k_pack<float2><<<nb, bs, 0, st>>>((const float2*)src, sd, g, dst, dst_prec, reunitarise);
     return cudaGetLastError();
 }
 
@@ -162,7 +162,7 @@ __global__ void k_fix_field(void* links, Geom g, int prec) {
 
 cudaError_t launch_fix_field(void* links, const Geom& g, int prec, cudaStream_t st) {
     const int64_t n = 4 * g.V;
-    k_fix_field<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(links, g, prec);
+    note_launch(), k_fix_field<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(links, g, prec);
     return cudaGetLastError();
 }
 
@@ -191,9 +191,9 @@ cudaError_t launch_unpack(const FieldRef& U, void* dst, int dst_dtype, cudaStrea
     const unsigned nb = (unsigned)((n + 255) / 256);
     FLUE_DISPATCH_LINKS(U, {
         if (dst_dtype == PREC_C128)
-            k_unpack<decltype(L), T, double2><<<nb, 256, 0, st>>>(L, U.g, (double2*)dst);
+            note_launch(), k_unpack<decltype(L), T, double2><<<nb, 256, 0, st>>>(L, U.g, (double2*)dst);
         else
-            k_unpack<decltype(L), T, float2><<<nb, 256, 0, st>>>(L, U.g, (float2*)dst);
+            note_launch(), k_unpack<decltype(L), T, float2><<<nb, 256, 0, st>>>(L, U.g, (float2*)dst);
     });
     return cudaGetLastError();
 }
@@ -236,9 +236,9 @@ __global__ void k_matmul_batch(const typename V2<T>::type* __restrict__ l, const
 cudaError_t launch_matmul_batch(const void* l, const void* r, void* o, int64_t n, int dtype, int dagger, cudaStream_t st) {
     const unsigned nb = (unsigned)((n + 127) / 128);
     if (dtype == PREC_C128)
-        k_matmul_batch<double><<<nb, 128, 0, st>>>((const double2*)l, (const double2*)r, (double2*)o, n, dagger);
+        note_launch(), k_matmul_batch<double><<<nb, 128, 0, st>>>((const double2*)l, (const double2*)r, (double2*)o, n, dagger);
     else
-        k_matmul_batch<float><<<nb, 128, 0, st>>>((const float2*)l, (const float2*)r, (float2*)o, n, dagger);
+        note_launch(), k_matmul_batch<float><<<nb, 128, 0, st>>>((const float2*)l, (const float2*)r, (float2*)o, n, dagger);
     return cudaGetLastError();
 }
 
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(RED_BS) k_plaquette(L U, Geom g, int mu0, int 
 
 cudaError_t launch_plaquette(const FieldRef& U, int mu0, int mu1, int nu1, double* part, double* out, cudaStream_t st) {
     const int nb = plaquette_blocks(U.g);
-    FLUE_DISPATCH_LINKS(U, k_plaquette<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, mu0, mu1, nu1, part));
+    FLUE_DISPATCH_LINKS(U, note_launch(), k_plaquette<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, mu0, mu1, nu1, part));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_finish_sums(part, nb, 1, out, st);
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(RED_BS) k_polyakov(L U, Geom g, double* __rest
 
 cudaError_t launch_polyakov(const FieldRef& U, double* part, double* out2, cudaStream_t st) {
     const int nb = polyakov_blocks(U.g);
-    FLUE_DISPATCH_LINKS(U, k_polyakov<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, part));
+    FLUE_DISPATCH_LINKS(U, note_launch(), k_polyakov<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, part));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_finish_sums(part, nb, 2, out2, st);
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(RED_BS)
 cudaError_t launch_wloop(const FieldRef& U, int tau, int mu, int nu, int nmu, int nnu, double* part, double* out,
                          cudaStream_t st) {
     const int nb = wloop_blocks(U.g);
-    FLUE_DISPATCH_LINKS(U, k_wloop<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, tau, mu, nu, nmu, nnu, part));
+    FLUE_DISPATCH_LINKS(U, note_launch(), k_wloop<decltype(L), T><<<nb, RED_BS, 0, st>>>(L, U.g, tau, mu, nu, nmu, nnu, part));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const double norm = tau < 0 ? (double)U.g.V : (double)(U.g.V / U.g.n[0]);
@@ -422,7 +422,7 @@ cudaError_t launch_genericpath(const FieldRef& U, const int* path_host, int npat
              U.g.st[3] * (coord_host[3] - 1);
     }
     const unsigned nb = coord_host ? 1u : (unsigned)((U.g.V + 127) / 128);
-    FLUE_DISPATCH_LINKS(U, k_genericpath<decltype(L), T><<<nb, 128, 0, st>>>(L, U.g, pa, ss, (typename V2<T>::type*)out));
+    FLUE_DISPATCH_LINKS(U, note_launch(), k_genericpath<decltype(L), T><<<nb, 128, 0, st>>>(L, U.g, pa, ss, (typename V2<T>::type*)out));
     return cudaGetLastError();
 }
 
@@ -472,9 +472,9 @@ cudaError_t launch_meanlink(const FieldRef& U, const void* G, int g_dtype, doubl
     const int nb = meanlink_blocks(U.g);
     FLUE_DISPATCH_LINKS(U, {
         if (g_dtype == PREC_C128)
-            k_meanlink<decltype(L), T, double2><<<nb, RED_BS, 0, st>>>(L, U.g, (const double2*)G, part);
+            note_launch(), k_meanlink<decltype(L), T, double2><<<nb, RED_BS, 0, st>>>(L, U.g, (const double2*)G, part);
         else
-            k_meanlink<decltype(L), T, float2><<<nb, RED_BS, 0, st>>>(L, U.g, (const float2*)G, part);
+            note_launch(), k_meanlink<decltype(L), T, float2><<<nb, RED_BS, 0, st>>>(L, U.g, (const float2*)G, part);
     });
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

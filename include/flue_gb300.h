@@ -107,6 +107,10 @@ const char *flue_last_error_detail(void);
  * up to max_stages durations in ms.  Process-wide, one device. */
 int flue_stage_timing(int enable);
 int flue_stage_times(double *ms, int max_stages, int *n_stages);
+/* Number of GPU kernels this library has launched in this process (all
+ * devices; a replayed ensemble graph counts its two kernels).  For launch
+ * accounting by benchmarks and tests; no reference counterpart. */
+uint64_t flue_kernel_launches(void);
 
 /* ======================================================================== */
 /* Tier 2: device entry points                                              */

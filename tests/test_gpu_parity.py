@@ -215,3 +215,14 @@ def test_host_buffer_tier():
     assert np.abs(u0 - oracle.uzerobar(U, gt)).max() < 1e-12
     # errors come back as status codes
     assert L.flue_plaquette_c(d, nt, nx, ny, nz, 0, 4, 4, ctypes.byref(s), ctypes.byref(n), ctypes.byref(t)) != 0
+
+
+def test_kernel_launch_counter():
+    """flue_kernel_launches counts the kernels a call runs: the plaquette is
+    one reduction kernel and its finisher."""
+    f = GaugeField.from_array(generate.random_field((4, 4, 4, 4), 0.3, 12))
+    L = _lib.load()
+    G.plaquette(f, 1, 4, 4)
+    n0 = L.flue_kernel_launches()
+    G.plaquette(f, 1, 4, 4)
+    assert L.flue_kernel_launches() - n0 == 2
