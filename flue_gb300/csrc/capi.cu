@@ -411,12 +411,15 @@ struct DevCache {
     cudaEvent_t cev[kCopyStreams + 1] = {};
     // T-slab pipeline of the host-buffer B^2 force (created on first use):
     // high-priority streams that stream slabs in (pack) and gradients out
-    // beside the compute on `st`, two buffer slots (packed slab + workspace)
+    // beside the compute on `st` (and up to kPipeComp - 1 more compute
+    // streams), a ring of kPipeComp + 1 buffer slots (packed slab + workspace)
+    static constexpr int kPipeComp = 3, kPipeSlots = kPipeComp + 1;
     bool pipe_init = false;
-    cudaStream_t s_in = nullptr, s_out = nullptr;
-    cudaEvent_t ev_go = nullptr, ev_in[2] = {}, ev_cp[2] = {}, ev_out[2] = {};
-    void* slot[2] = {};
-    size_t slot_bytes[2] = {};
+    cudaStream_t s_in = nullptr, s_out = nullptr, s_cp[kPipeComp - 1] = {};
+    cudaEvent_t ev_go = nullptr, ev_in[kPipeSlots] = {}, ev_cp[kPipeSlots] = {}, ev_out[kPipeSlots] = {},
+                ev_end[kPipeComp - 1] = {};
+    void* slot[kPipeSlots] = {};
+    size_t slot_bytes[kPipeSlots] = {};
 };
 
 // A device-usable address of host memory `p`, or NULL: pinned (page-locked,
@@ -557,8 +560,9 @@ double elapsed_s(DevCache* c) {
 // Host-buffer B^2 and gradient, pipelined over time slabs.  B^2 uses only
 // spatial planes, so time slices are independent: slab k (nts time slices)
 // is packed from host memory on s_in, computed (lines, forward, line
-// cotangents) on st, and its link cotangents are written into the host
-// gradient on s_out, while slab k+1 is packed and slab k-1 written out.
+// cotangents) on compute stream k % ncomp, and its link cotangents are
+// written into the host gradient on s_out, while later slabs are packed and
+// earlier ones written out.
 // The two I/O streams have the highest priority and capped grids, so they
 // take a few SMs and the host link (NVLink-C2C) while compute keeps the rest.
 // Per-slab B^2 partials are added on the host in slab order (deterministic).
@@ -569,10 +573,14 @@ int pipe_setup(DevCache* c) {
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->s_in, cudaStreamNonBlocking, hi);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->s_out, cudaStreamNonBlocking, hi);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_go, cudaEventDisableTiming);
-    for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+    for (int j = 0; j < DevCache::kPipeSlots && e == cudaSuccess; ++j) {
         e = cudaEventCreateWithFlags(&c->ev_in[j], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_cp[j], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out[j], cudaEventDisableTiming);
+    }
+    for (int i = 0; i < DevCache::kPipeComp - 1 && e == cudaSuccess; ++i) {
+        e = cudaStreamCreateWithFlags(&c->s_cp[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_end[i], cudaEventDisableTiming);
     }
     if (e != cudaSuccess) return cuda_status(e);
     c->pipe_init = true;
@@ -613,38 +621,46 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
     const Geom g0 = make_geom(nts, NX, NY, NZ);
     const size_t fbytes = ((size_t)flue_field_bytes(nts, NX, NY, NZ, prec) + 255) & ~(size_t)255;
     const size_t wbytes = energy_ws_bytes(g0, prec, ps, d_grad != nullptr);
-    for (int j = 0; j < 2; ++j)
+    // compute streams (FLUE_PIPE_STREAMS, default 3): slab k computes on
+    // stream k % ncomp, so the compute of neighbouring slabs overlaps too
+    // (measured at 64x32^3, 8 slabs: 12.5 ms on 1 stream, 11.9 on 2, 11.8 on 3)
+    int ncomp = env_int("FLUE_PIPE_STREAMS", 3);
+    ncomp = ncomp < 1 ? 1 : (ncomp > DevCache::kPipeComp ? DevCache::kPipeComp : ncomp);
+    const int nslot = ncomp + 1;
+    for (int j = 0; j < nslot; ++j)
         if ((rc = grow(&c->slot[j], &c->slot_bytes[j], fbytes + wbytes))) return rc;
     // grid caps of the I/O kernels (FLUE_IN_BLOCKS, FLUE_OUT_BLOCKS): measured
-    // on GB300 at 64x32^3, 8 slabs: 32 pack blocks of 256 threads and 16 x 4
-    // output blocks of 128 give 12.4 ms per call against 16.9 ms unpipelined;
-    // uncapped I/O grids take every SM and serialise with compute (16.9 ms),
-    // 8 / 4 starve the host link (22 ms)
+    // on GB300 at 64x32^3, 8 slabs, one compute stream: 32 pack blocks of 256
+    // threads and 16 x 4 output blocks of 128 give 12.4 ms per call against
+    // 16.9 ms unpipelined; uncapped I/O grids take every SM and serialise with
+    // compute (16.9 ms), 8 / 4 starve the host link (22 ms)
     const unsigned in_blocks = (unsigned)env_int("FLUE_IN_BLOCKS", 32);
     const unsigned out_blocks = (unsigned)env_int("FLUE_OUT_BLOCKS", 16);
     const size_t esz = data_dtype == FLUE_C128 ? 16 : 8;
     cudaError_t e = cudaEventRecord(c->ev_go, c->st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_in, c->ev_go, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_out, c->ev_go, 0);
+    for (int i = 1; i < ncomp && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(c->s_cp[i - 1], c->ev_go, 0);
     for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
-        const int j = k & 1, t0 = k * nts, n = NT - t0 < nts ? NT - t0 : nts;
+        const int j = k % nslot, t0 = k * nts, n = NT - t0 < nts ? NT - t0 : nts;
+        cudaStream_t cs = (k % ncomp) == 0 ? c->st : c->s_cp[k % ncomp - 1];
         const Geom g = make_geom(n, NX, NY, NZ);
         char* buf = (char*)c->slot[j];
         const FieldRef U{buf, g, prec};
-        // pack slab k once the compute of slab k-2 has read this slot
-        if (k >= 2 && (e = cudaStreamWaitEvent(c->s_in, c->ev_cp[j], 0)) != cudaSuccess) break;
+        // pack slab k once the compute of slab k - nslot has read this slot
+        if (k >= nslot && (e = cudaStreamWaitEvent(c->s_in, c->ev_cp[j], 0)) != cudaSuccess) break;
         if ((e = launch_pack((const char*)d_in + (size_t)t0 * esz, data_dtype, st, g, buf, prec, 0, c->s_in,
                              in_blocks)) != cudaSuccess)
             break;
         if ((e = cudaEventRecord(c->ev_in[j], c->s_in)) != cudaSuccess) break;
-        // compute slab k once it is packed and the output of slab k-2 has
-        // left this slot's workspace
-        if ((e = cudaStreamWaitEvent(c->st, c->ev_in[j], 0)) != cudaSuccess) break;
-        if (k >= 2 && d_grad && (e = cudaStreamWaitEvent(c->st, c->ev_out[j], 0)) != cudaSuccess) break;
-        if ((e = launch_energy_slab_fwd(U, 0, n, ps, V, c->scal + k, d_grad != nullptr, buf + fbytes, wbytes,
-                                        c->st)) != cudaSuccess)
+        // compute slab k once it is packed and the output of slab k - nslot
+        // has left this slot's workspace
+        if ((e = cudaStreamWaitEvent(cs, c->ev_in[j], 0)) != cudaSuccess) break;
+        if (k >= nslot && d_grad && (e = cudaStreamWaitEvent(cs, c->ev_out[j], 0)) != cudaSuccess) break;
+        if ((e = launch_energy_slab_fwd(U, 0, n, ps, V, c->scal + k, d_grad != nullptr, buf + fbytes, wbytes, cs)) !=
+            cudaSuccess)
             break;
-        if ((e = cudaEventRecord(c->ev_cp[j], c->st)) != cudaSuccess) break;
+        if ((e = cudaEventRecord(c->ev_cp[j], cs)) != cudaSuccess) break;
         if (!d_grad) continue;
         if ((e = cudaStreamWaitEvent(c->s_out, c->ev_cp[j], 0)) != cudaSuccess) break;
         if ((e = launch_energy_slab_out(U, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, out_blocks, c->s_out)) !=
@@ -652,12 +668,17 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
             break;
         if ((e = cudaEventRecord(c->ev_out[j], c->s_out)) != cudaSuccess) break;
     }
-    // everything joins st before the partials are read
-    for (int j = 0; j < 2 && e == cudaSuccess && d_grad; ++j)
-        if (j < nslab) e = cudaStreamWaitEvent(c->st, c->ev_out[j], 0);
+    // every stream joins st before the partials are read (also after an error)
+    for (int i = 1; i < ncomp; ++i) {
+        cudaError_t r = cudaEventRecord(c->ev_end[i - 1], c->s_cp[i - 1]);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(c->st, c->ev_end[i - 1], 0);
+        if (e == cudaSuccess) e = r;
+    }
+    if (e == cudaSuccess && d_grad) e = cudaStreamWaitEvent(c->st, c->ev_out[(nslab - 1) % nslot], 0);
     if (e != cudaSuccess) {
         cudaStreamSynchronize(c->s_in);
         cudaStreamSynchronize(c->s_out);
+        for (int i = 1; i < ncomp; ++i) cudaStreamSynchronize(c->s_cp[i - 1]);
         cudaStreamSynchronize(c->st);
         return cuda_status(e);
     }
@@ -931,7 +952,7 @@ void flue_release_host_cache(void) {
         if (c->out) cudaFree(c->out);
         c->field = c->field2 = c->ws = c->out = nullptr;
         c->field_bytes = c->field2_bytes = c->ws_bytes = c->out_bytes = 0;
-        for (int j = 0; j < 2; ++j) {
+        for (int j = 0; j < DevCache::kPipeSlots; ++j) {
             if (c->slot[j]) cudaFree(c->slot[j]);
             c->slot[j] = nullptr;
             c->slot_bytes[j] = 0;
