@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--ensemble", action="store_true",
                    help="also time the 96-field ensemble (plaquette/Polyakov/B^2 in one graph-captured launch)")
+    p.add_argument("--propagator", action="store_true",
+                   help="instead of the headline step, time the scalar gluon propagator (FFT pipeline) per precision")
     p.add_argument("--observables", action="store_true",
                    help="instead of the headline step, time every observable entry point (FP64 and FP32-r12)")
     return p.parse_args()
@@ -142,6 +144,53 @@ def observables_bench(dims, steps):
     return {"lattice": list(dims), "sites": V, "rows": rows,
             "note": "ms includes the host round trip of scalar results (tiny) and per-call launches; bytes are "
                     "algorithmic (links read once, outputs written once)"}
+
+
+def propagator_bench(dims, steps):
+    """Scalar gluon propagator D(q) on every momentum of `dims` (device-resident
+    field, FP64 output): ms per call and sites/s for c128 (FP64 transforms),
+    c64 and r12 (FP32 transforms).  `alg_bytes_per_site` = links read once +
+    D written once; `pipeline_bytes_per_site` = that plus the 32 colour fields
+    written, read by the time transform, its half spectrum written, read and
+    written by the (x,y,z) transform and read twice by the sum (the +-q reads)."""
+    import torch
+
+    from flue_gb300 import generate, gluonProp
+    from flue_gb300.field import GaugeField
+
+    nt, nx, ny, nz = dims
+    V = nt * nx * ny * nz
+    f64 = generate.random_field(dims, 0.3, 1, device="cuda")
+    fields = {"c128": f64, "c64": GaugeField.from_array(f64, prec="c64"), "r12": GaugeField.from_array(f64, prec="r12")}
+    link_b = {"c128": 144, "c64": 72, "r12": 48}
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    rows = []
+    for prec, f in fields.items():
+        es = 8 if prec == "c128" else 4
+        spec = 32 * (nt // 2 + 1) / nt * 2 * es  # half spectrum bytes per site
+        alg = 4 * link_b[prec] + 8
+        pipe = alg + 32 * es * 2 + spec * 4
+        for _ in range(3):
+            gluonProp.scalar_gluon_prop(f)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            gluonProp.scalar_gluon_prop(f)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        rows.append({"prec": prec, "ms": ms, "sites_per_s": V / (ms * 1e-3), "alg_bytes_per_site": alg,
+                     "pipeline_bytes_per_site": round(pipe, 1), "alg_GBps": alg * V / (ms * 1e-3) / 1e9,
+                     "pipeline_GBps": pipe * V / (ms * 1e-3) / 1e9,
+                     "pipeline_hbm_frac": pipe * V / (ms * 1e-3) / 1e9 / hbm})
+    return {"metric": "scalar gluon propagator D(q), all momenta", "lattice": list(dims), "sites": V,
+            "hbm_peak_gbs": hbm, "steps": steps, "rows": rows}
 
 
 def bench_config(args, dims, n_replicas):
@@ -362,6 +411,12 @@ def main():
         ws = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))
         run_reference(args, dims, ws, rank)
+        return
+    if args.propagator:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(propagator_bench(dims, max(3, min(args.steps, 20)))), flush=True)
         return
     if args.observables:
         import torch

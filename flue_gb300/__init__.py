@@ -7,8 +7,8 @@ Wilson flow, behind the reference's Python API (``FLUE.gluonCalc``).
 reference's names and calling conventions.  All arithmetic runs in the CUDA
 library ``libflue_gb300.so`` (C ABI in include/flue_gb300.h).
 """
-from . import _lib, field, generate, gluonCalc  # noqa: F401
+from . import _lib, field, generate, gluonAna, gluonCalc, gluonProp  # noqa: F401
 from .field import GaugeField  # noqa: F401
 
 __version__ = "0.1.0"
-__all__ = ["gluonCalc", "GaugeField", "field", "generate"]
+__all__ = ["gluonCalc", "gluonProp", "gluonAna", "GaugeField", "field", "generate"]

@@ -35,6 +35,7 @@ OP_ENERGY_FORCE = 6
 OP_PLAQUETTE_FORCE = 7
 OP_MEANLINK = 8
 OP_WFLOW = 9
+OP_GLUON_PROP = 10
 
 
 class FlueError(RuntimeError):
@@ -89,6 +90,8 @@ SIGNATURES = {
     "flue_plaquette_force": ([_FP, _P, _P, _I, _P, _SZ, _P], _I),
     "flue_meanlink": ([_FP, _P, _I, _P, _P, _SZ, _P], _I),
     "flue_wflow_step": ([_FP, _D, _P, _SZ, _P], _I),
+    "flue_gauge_transform": ([_FP, _P, _I, _P], _I),
+    "flue_gluon_propagator": ([_FP, _D, _I, _P, _P, _SZ, _P], _I),
     "flue_plaquette_c": ([_P, _I, _I, _I, _I, _I, _I, _I, _P, _P, _P], _I),
     "flue_genplaquette_c": ([_P, _I, _I, _I, _I, _I, _I, _I, _P, _P, _P], _I),
     "flue_polyakov_c": ([_P, _I, _I, _I, _I, _P, _P, _P], _I),
@@ -101,6 +104,7 @@ SIGNATURES = {
     "flue_multiplymatmat_c": ([_P, _P, _P], _I),
     "flue_fixsu3matrix_c": ([_P], _I),
     "flue_uzerobar_c": ([_P, _I, _I, _I, _I, _P, _P], _I),
+    "flue_scalargluonprop_c": ([_I, _I, _P, _D, _P], _I),
     "flue_magnetic_force_c": ([_P, _I, _I, _I, _I, _I, _I, _I, _P, _P], _I),
     "flue_release_host_cache": ([], None),
     "flue_ensemble_create": ([_P, _FP, _I, _I, _I, _I, _I], _I),

@@ -73,7 +73,10 @@ def build(force: bool = False, verbose: bool = False, extra_flags=(), lib_path: 
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = lib + f".tmp{os.getpid()}"
-    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs]
+    # cuFFT (the gluon propagator's transforms), found at run time through the
+    # toolkit's library directory
+    cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(cc))), "lib64")
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcufft", "-Xlinker", "-rpath", "-Xlinker", cudalib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stderr}")

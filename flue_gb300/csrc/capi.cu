@@ -100,6 +100,8 @@ size_t ws_bytes_for(int op, const Geom& g, int prec) {
             return a256((size_t)meanlink_blocks(g) * 4 * 8);
         case FLUE_OP_WFLOW:
             return wflow_ws_bytes(g);
+        case FLUE_OP_GLUON_PROP:
+            return gluon_prop_ws_bytes(g, prec);
         default:
             return 0;
     }
@@ -370,6 +372,28 @@ int flue_meanlink(const flue_field* U, const void* G, int g_dtype, double* d_sum
     if (g_dtype != FLUE_C128 && g_dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "G must be c128 or c64");
     if ((rc = check_ws(FLUE_OP_MEANLINK, F, ws_bytes, ws))) return rc;
     return cuda_status(launch_meanlink(F, G, g_dtype, (double*)ws, d_sum4, (cudaStream_t)stream));
+}
+
+int flue_gauge_transform(const flue_field* U, const void* G, int g_dtype, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!G) return fail(FLUE_ERR_ARG, "NULL gauge transformation");
+    if (g_dtype != FLUE_C128 && g_dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "G must be c128 or c64");
+    if (((uintptr_t)G) % (g_dtype == FLUE_C64 ? 8 : 16)) return fail(FLUE_ERR_LAYOUT, "G pointer misaligned");
+    return cuda_status(launch_gauge_transform(F, G, g_dtype, (cudaStream_t)stream));
+}
+
+int flue_gluon_propagator(const flue_field* U, double xi, int mu_start, double* d_D, void* ws, size_t ws_bytes,
+                          void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_D) return fail(FLUE_ERR_ARG, "NULL output");
+    if (mu_start != 0 && mu_start != 1) return fail(FLUE_ERR_ARG, "mu_start must be 0 (all directions) or 1 (spatial)");
+    if (!isfinite(xi)) return fail(FLUE_ERR_ARG, "xi must be finite");
+    if ((rc = check_ws(FLUE_OP_GLUON_PROP, F, ws_bytes, ws))) return rc;
+    return cuda_status(launch_gluon_propagator(F, xi, mu_start, d_D, ws, ws_bytes, (cudaStream_t)stream));
 }
 
 int flue_wflow_step(const flue_field* U, double eps, void* ws, size_t ws_bytes, void* stream) {
@@ -880,6 +904,18 @@ int flue_uzerobar_c(const double* data, int NT, int NX, int NY, int NZ, const do
         u0[3] = u0[4] = u0[5] = NAN;
     }
     return FLUE_OK;
+}
+
+int flue_scalargluonprop_c(int NS, int NT, const void* U, double xi, double* D) {
+    if (!U || !D) return fail(FLUE_ERR_ARG, "NULL pointer");
+    HOST_PROLOGUE();
+    flue_field F;
+    if ((rc = upload_c128(c, (const double*)U, NT, NS, NS, NS, &F))) return rc;
+    if ((rc = ensure_ws(c, FLUE_OP_GLUON_PROP, F))) return rc;
+    const size_t db = (size_t)NT * NS * NS * NS * sizeof(double);
+    if ((rc = grow(&c->out, &c->out_bytes, db))) return rc;
+    if ((rc = flue_gluon_propagator(&F, xi, 0, (double*)c->out, c->ws, c->ws_bytes, c->st))) return rc;
+    return fetch(c, D, c->out, db);
 }
 
 int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int NY, int NZ, int prec, int force_form,

@@ -16,6 +16,25 @@ struct FieldRef {
     int prec;
 };
 
+// Runs the statements with `T` (compute type) and `L` (link accessor) bound
+// for the precision of FieldRef U.
+#define FLUE_DISPATCH_LINKS(U, ...)                                              \
+    do {                                                                         \
+        if ((U).prec == PREC_C128) {                                             \
+            using T = double;                                                    \
+            FullLinks<double> L{(const double2*)(U).links, (U).g.V};             \
+            __VA_ARGS__;                                                         \
+        } else if ((U).prec == PREC_C64) {                                       \
+            using T = float;                                                     \
+            FullLinks<float> L{(const float2*)(U).links, (U).g.V};               \
+            __VA_ARGS__;                                                         \
+        } else {                                                                 \
+            using T = float;                                                     \
+            R12Links L{(const float4*)(U).links, (U).g.V};                       \
+            __VA_ARGS__;                                                         \
+        }                                                                        \
+    } while (0)
+
 // reduction finisher: out[j] = sum_i partial[j*nparts + i], j < nout
 cudaError_t launch_finish_sums(const double* partial, int nparts, int nout, double* out, cudaStream_t st,
                                double scale = 1.0);
@@ -88,5 +107,11 @@ cudaError_t stage_times(double* ms, int maxn, int* n);
 // Wilson flow (flow.cu)
 size_t wflow_ws_bytes(const Geom& g);
 cudaError_t launch_wflow_step(void* links, const Geom& g, int prec, double eps, void* ws, cudaStream_t st);
+
+// gauge transformation and gluon propagator (propagator.cu)
+cudaError_t launch_gauge_transform(const FieldRef& U, const void* G, int g_dtype, cudaStream_t st);
+size_t gluon_prop_ws_bytes(const Geom& g, int prec);
+cudaError_t launch_gluon_propagator(const FieldRef& U, double xi, int mu_start, double* D, void* ws, size_t ws_bytes,
+                                    cudaStream_t st);
 
 }  // namespace flue

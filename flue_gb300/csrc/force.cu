@@ -36,23 +36,6 @@
 
 namespace flue {
 
-#define FLUE_DISPATCH_LINKS(U, ...)                                              \
-    do {                                                                         \
-        if ((U).prec == PREC_C128) {                                             \
-            using T = double;                                                    \
-            FullLinks<double> L{(const double2*)(U).links, (U).g.V};             \
-            __VA_ARGS__;                                                         \
-        } else if ((U).prec == PREC_C64) {                                       \
-            using T = float;                                                     \
-            FullLinks<float> L{(const float2*)(U).links, (U).g.V};               \
-            __VA_ARGS__;                                                         \
-        } else {                                                                 \
-            using T = float;                                                     \
-            R12Links L{(const float4*)(U).links, (U).g.V};                       \
-            __VA_ARGS__;                                                         \
-        }                                                                        \
-    } while (0)
-
 // 5-loop coefficients, src/wloops.F90:219-224 (k5 = 1/180).
 constexpr double K5c = 1.0 / 180.0;
 constexpr double K1c = (19.0 / 9.0) - 55.0 * K5c;

@@ -11,26 +11,6 @@
 
 namespace flue {
 
-// ---------------------------------------------------------------------------
-// precision dispatch
-// ---------------------------------------------------------------------------
-#define FLUE_DISPATCH_LINKS(U, ...)                                              \
-    do {                                                                         \
-        if ((U).prec == PREC_C128) {                                             \
-            using T = double;                                                    \
-            FullLinks<double> L{(const double2*)(U).links, (U).g.V};             \
-            __VA_ARGS__;                                                         \
-        } else if ((U).prec == PREC_C64) {                                       \
-            using T = float;                                                     \
-            FullLinks<float> L{(const float2*)(U).links, (U).g.V};               \
-            __VA_ARGS__;                                                         \
-        } else {                                                                 \
-            using T = float;                                                     \
-            R12Links L{(const float4*)(U).links, (U).g.V};                       \
-            __VA_ARGS__;                                                         \
-        }                                                                        \
-    } while (0)
-
 static inline int grid_for(int64_t n, int bs, int cap) {
     int64_t b = (n + bs - 1) / bs;
     if (b > cap) b = cap;

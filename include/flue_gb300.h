@@ -84,6 +84,7 @@ extern "C" {
 #define FLUE_OP_PLAQUETTE_FORCE 7
 #define FLUE_OP_MEANLINK 8
 #define FLUE_OP_WFLOW 9
+#define FLUE_OP_GLUON_PROP 10    /* scalar gluon propagator (FFT buffers + cuFFT work area) */
 
 typedef struct flue_field {
     const void *links; /* device pointer, layout given by prec */
@@ -184,6 +185,28 @@ int flue_meanlink(const flue_field *U, const void *G, int g_dtype, double *d_sum
 /* One Luescher RK3 step of the Wilson flow with step eps, in place; the
  * field must be FLUE_C128 or FLUE_C64. */
 int flue_wflow_step(const flue_field *U, double eps, void *ws, size_t ws_bytes, void *stream);
+/* Gauge transformation in place: U_mu(x) <- G(x) U_mu(x) G(x+mu)^+ for a
+ * device G of layout (NT,NX,NY,NZ,3,3), complex128 or complex64 (g_dtype);
+ * applies the Landau-gauge transformation that ReadGaugeTransformation_cola
+ * reads (src/gaugeIO/ILDG_bin.f90:65-105) before a propagator measurement.
+ * G must be SU(3) (an R12 field keeps two rows). */
+int flue_gauge_transform(const flue_field *U, const void *G, int g_dtype, void *stream);
+/* Scalar gluon propagator on every lattice momentum (the observable that
+ * src/gluonCalc/gluonProp.f90 works towards, defined as in hep-lat/9803105,
+ * which that file cites; the reference's routines are unfinished):
+ *   A_mu(x) = [U_mu(x) - U_mu(x)^+]/(2i) - trace/3,  A^a = Tr(A lambda^a),
+ *   A^a_mu(q) = sum_x exp(-i q.x) A^a_mu(x),  q_mu = 2 pi n_mu / N_mu,
+ *   D(q) = sum_{mu >= mu_start} w_mu sum_a |A^a_mu(q)|^2 / (8 n(q) V),
+ * w_t = xi^2 (anisotropy, as gluonProp.f90:186-190), w_i = 1, n(0) = 4,
+ * n(q != 0) = 3 (gluonProp.f90:208-236); mu_start = 0 sums all four
+ * directions, 1 the spatial ones.  The phase exp(-i q_mu/2) of the
+ * midpoint convention has modulus 1 and drops out.  d_D: FP64
+ * (NT,NX,NY,NZ), index n_mu = 0..N_mu-1 (n_mu > N_mu/2: negative q).  The
+ * field should be Landau-gauge fixed (flue_gauge_transform).  Transforms by
+ * cuFFT in the field's compute precision; scratch flue_workspace_bytes(
+ * FLUE_OP_GLUON_PROP, ...). */
+int flue_gluon_propagator(const flue_field *U, double xi, int mu_start, double *d_D, void *ws, size_t ws_bytes,
+                          void *stream);
 
 /* ---- ensemble batching (no reference counterpart; the reference's
  * magnetic app loops over configurations one by one, app/magnetic.f90:109-140)
@@ -261,6 +284,12 @@ int flue_fixsu3matrix_c(double *U_x);
  * all, spatial and temporal links with U'_mu(x) = G(x) U_mu(x) G(x+mu)^+ when
  * G (host complex128 (NT,NX,NY,NZ,3,3), Fortran order) is given, else NaN. */
 int flue_uzerobar_c(const double *data, int NT, int NX, int NY, int NZ, const double *G, double *u0);
+/* scalarGluonProp_c (c_wrapper/FLUE_c.f90:9-16, src/gluonCalc/gluonProp.f90:17-112):
+ * same arguments -- NS, NT, host complex128 U(NT,NS,NS,NS,4,3,3) in position
+ * space, anisotropy xi -- and D the propagator of flue_gluon_propagator with
+ * mu_start = 0, host FP64 of shape (NT,NS,NS,NS) (the reference declares
+ * (NS,NS,NS,NS), which holds it only when NT = NS). */
+int flue_scalargluonprop_c(int NS, int NT, const void *U, double xi, double *D);
 /* B^2 forward + backward from host buffers: data is complex128
  * (data_dtype FLUE_C128) or complex64 (FLUE_C64), computed in precision
  * prec; grad (host, same layout and dtype as data) receives the gradient
