@@ -474,6 +474,9 @@ static const void* device_view(const void* p) {
 // c->st before the call, and everything queued after it waits for all chunks).
 static cudaError_t copy_async(DevCache* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
     const size_t kMinSplit = (size_t)64 << 20;
+    const char* env = getenv("FLUE_COPY_STREAMS");  // read per call: 1 = one copy
+    const int n = env ? atoi(env) : DevCache::kCopyStreams;
+    c->ncopy = n < 1 ? 1 : (n > DevCache::kCopyStreams ? DevCache::kCopyStreams : n);
     if (c->ncopy <= 1 || bytes < kMinSplit) return cudaMemcpyAsync(dst, src, bytes, kind, c->st);
     cudaError_t e = cudaEventRecord(c->cev[0], c->st);
     if (e != cudaSuccess) return e;
@@ -526,15 +529,12 @@ DevCache* cache_for_current(int* rc) {
             *rc = cuda_status(e);
             return nullptr;
         }
-        const char* env = getenv("FLUE_COPY_STREAMS");
-        int n = env ? atoi(env) : DevCache::kCopyStreams;
-        c->ncopy = n < 1 ? 1 : (n > DevCache::kCopyStreams ? DevCache::kCopyStreams : n);
-        for (int k = 0; k < DevCache::kCopyStreams && c->ncopy > 1; ++k)
+        for (int k = 0; k < DevCache::kCopyStreams; ++k)
             if ((e = cudaStreamCreateWithFlags(&c->cst[k], cudaStreamNonBlocking)) != cudaSuccess) {
                 *rc = cuda_status(e);
                 return nullptr;
             }
-        for (int k = 0; k <= DevCache::kCopyStreams && c->ncopy > 1; ++k)
+        for (int k = 0; k <= DevCache::kCopyStreams; ++k)
             if ((e = cudaEventCreateWithFlags(&c->cev[k], cudaEventDisableTiming)) != cudaSuccess) {
                 *rc = cuda_status(e);
                 return nullptr;

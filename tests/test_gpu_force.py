@@ -188,3 +188,37 @@ def test_device_force_time_slabs(slabs, streams, monkeypatch):
     e, h = forces.loop5_energy_force(f, ((3, 2), (4, 2)))
     assert abs(e - e1) < 1e-12 * abs(e1)
     assert np.array_equal(_np(h), h1)
+
+
+@pytest.mark.parametrize("copy_streams", ["1", "4"])
+def test_host_buffer_force_staged_copies(copy_streams, monkeypatch):
+    """With zero-copy turned off (FLUE_ZERO_COPY=0) the host-buffer force
+    goes through library device buffers; a 127 MB field takes the chunked
+    multi-stream copy path.  Its gradient equals the zero-copy pipeline's
+    bit for bit, B^2 to FP64 summation order."""
+    import ctypes
+
+    from flue_gb300 import _lib
+
+    dims = (32, 24, 24, 24)
+    f = generate.random_field(dims, 0.3, 21, device="cuda")
+    host = GaugeField.from_array(f, prec="c64").to_tensor(torch.complex64).permute(6, 5, 4, 3, 2, 1, 0)
+    host = host.contiguous().cpu().pin_memory()
+    assert host.numel() * 8 > 64 << 20
+    L = _lib.load()
+
+    def run():
+        grad = torch.full_like(host, float("nan")).pin_memory()
+        b = ctypes.c_double()
+        rc = L.flue_magnetic_force_c(ctypes.c_void_p(host.data_ptr()), _lib.C64, *dims, _lib.R12, _lib.FORCE_LIE,
+                                     ctypes.byref(b), ctypes.c_void_p(grad.data_ptr()))
+        assert rc == 0, L.flue_last_error_detail()
+        return b.value, grad
+
+    b_zc, g_zc = run()
+    monkeypatch.setenv("FLUE_ZERO_COPY", "0")
+    monkeypatch.setenv("FLUE_COPY_STREAMS", copy_streams)
+    b_st, g_st = run()
+    L.flue_release_host_cache()
+    assert abs(b_st - b_zc) < 1e-12 * abs(b_zc)
+    assert torch.equal(g_st, g_zc)
