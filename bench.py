@@ -221,24 +221,38 @@ def ensemble_bench(steps: int):
     cands = [(t, b, m) for t in (2, 8, 32) for b in (128, 256) for m in (1, 4)]
     cfg = E.autotune(f32, candidates=cands, reps=1)
     b2s = {}
-    for name, fs, nrep in (("fp32", f32, steps), ("fp64", f64, 1)):
-        ens = E.Ensemble(fs, tile=cfg[0], block=cfg[1], blocks_per_sm=cfg[2])
+    from flue_gb300 import _lib
+
+    L = _lib.load()
+    runs = (("fp32", f32, steps, "persistent"), ("fp64", f64, 1, "persistent"), ("fp32_pipeline", f32, steps, "pipeline"),
+            ("fp64_pipeline", f64, 1, "pipeline"))
+    for name, fs, nrep, mode in runs:
+        if mode == "pipeline":
+            ens = E.Ensemble(fs, mode="pipeline")
+        else:
+            ens = E.Ensemble(fs, tile=cfg[0], block=cfg[1], blocks_per_sm=cfg[2])
         ens.capture()
         ens.launch()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = L.flue_kernel_launches()
         e0.record()
         for _ in range(nrep):
             ens.launch()
         e1.record()
         torch.cuda.synchronize()
+        nl = (L.flue_kernel_launches() - n0) // nrep
         ms = e0.elapsed_time(e1) / nrep
         b2 = ens.out[:, 4].cpu().numpy()
         b2s[name] = b2
-        out[name] = {"ms_per_eval": ms, "sites_per_s": sites / (ms * 1e-3), "fields_per_s": len(dims) / (ms * 1e-3),
-                     "items": ens.items, "config": {"tile_cols": cfg[0], "block": cfg[1], "blocks_per_sm": cfg[2]},
-                     "b2_first": float(b2[0]), "launches_per_eval": 3}
+        out[name] = {"mode": mode, "ms_per_eval": ms, "sites_per_s": sites / (ms * 1e-3),
+                     "fields_per_s": len(dims) / (ms * 1e-3), "b2_first": float(b2[0]), "kernels_per_eval": int(nl)}
+        if mode == "persistent":
+            out[name].update({"items": ens.items,
+                              "config": {"tile_cols": cfg[0], "block": cfg[1], "blocks_per_sm": cfg[2]}})
         ens.close()
+    out["b2_rel_pipeline_persistent_fp64_max"] = float(
+        max(abs(a - b) / abs(b) for a, b in zip(b2s["fp64_pipeline"], b2s["fp64"])))
     out["b2_rel_fp32_fp64_max"] = float(max(abs(a - b) / abs(b) for a, b in zip(b2s["fp32"], b2s["fp64"])))
     return out
 

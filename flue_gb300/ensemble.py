@@ -6,7 +6,8 @@ configurations one at a time, app/magnetic.f90:109-140).
 * :class:`Ensemble` -- device work list over a list of
   :class:`~flue_gb300.field.GaugeField` of one precision; ``run()`` replays a
   CUDA graph (memset of the work counter + persistent kernel + per-field
-  finisher) and returns per-field observables.
+  finisher, or in pipeline mode the per-field kernel pipelines) and returns
+  per-field observables.
 * :func:`autotune` -- the project's tile tuner: times candidate (columns per
   item, block size, blocks per SM) on the actual ensemble and caches the
   winner in a JSON file keyed by GPU name and ensemble signature.
@@ -47,8 +48,15 @@ def _signature(fields: Sequence[GaugeField], with_b2: bool) -> str:
 
 
 class Ensemble:
+    """``mode="persistent"`` (default): one persistent launch over all
+    fields' work items (leaves walked link by link, no scratch).
+    ``mode="pipeline"``: per field the device entry points (plaquettes,
+    Polyakov loop, line-based B^2 on time slabs) with one library
+    workspace of the largest field's size, all captured into one graph;
+    same outputs, several kernels per field."""
+
     def __init__(self, fields: Sequence[GaugeField], tile=None, block=256, blocks_per_sm=2, with_b2=True,
-                 tune=False):
+                 tune=False, mode="persistent"):
         if not fields:
             raise ValueError("empty ensemble")
         precs = {f.prec for f in fields}
@@ -57,7 +65,12 @@ class Ensemble:
         self.fields = list(fields)
         self.with_b2 = bool(with_b2)
         self.device = fields[0].device
-        if tune:
+        if mode not in ("persistent", "pipeline"):
+            raise ValueError("mode must be 'persistent' or 'pipeline'")
+        self.mode = mode
+        if mode == "pipeline":
+            tile = 0  # the C ABI's pipeline mode
+        elif tune:
             tile, block, blocks_per_sm = autotune(self.fields, with_b2=self.with_b2)
         elif tile is None:
             tile = 4

@@ -220,7 +220,13 @@ int flue_gluon_propagator(const flue_field *U, double xi, int mu_start, double *
  * temporal planes, sum Re Tr and Im Tr of the Polyakov loop, B^2 (divided by
  * V; 0 when with_b2 = 0), V.  create() allocates the work list and partials
  * on the current device (library-owned); capture() records memset + kernel +
- * finisher writing to d_out into a CUDA graph, replay() launches it. */
+ * finisher writing to d_out into a CUDA graph, replay() launches it.
+ * tile_cols = 0 selects pipeline mode instead (block, blocks_per_sm unused):
+ * per field the device entry points -- flue_plaquette (spatial, temporal),
+ * flue_polyakov, flue_magnetic (line-based, time slabs) -- with one
+ * library-owned workspace for the largest field, the same outputs; capture()
+ * then runs one evaluation uncaptured first (the entry points set up their
+ * library streams on first use) and records every field's kernels. */
 typedef struct flue_ensemble flue_ensemble;
 int flue_ensemble_create(flue_ensemble **e, const flue_field *fields, int nfields, int tile_cols, int block,
                          int blocks_per_sm, int with_b2);
