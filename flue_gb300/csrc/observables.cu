@@ -230,21 +230,35 @@ constexpr int RED_BS = 256;
 
 int plaquette_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
 
+// FP32: at most 128 registers (two 256-thread blocks per SM): measured on
+// GB300 at 32^3x64, all planes, c64 0.53 -> 0.36 ms per call against the
+// unbounded unrolled kernel's 0.45 ms; FP64 keeps its registers (bound by the
+// FP64 pipe, it spills under the cap)
+#ifndef FLUE_PLAQ_MINB
+#define FLUE_PLAQ_MINB 2
+#endif
 template <class L, typename T>
-__global__ void __launch_bounds__(RED_BS) k_plaquette(L U, Geom g, int mu0, int mu1, int nu1, double* __restrict__ part) {
+__global__ void __launch_bounds__(RED_BS, sizeof(T) == 4 ? FLUE_PLAQ_MINB : 1)
+    k_plaquette(L U, Geom g, int mu0, int mu1, int nu1, double* __restrict__ part) {
     __shared__ double sh[32];
     double acc = 0.0;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < g.V; s += (int64_t)gridDim.x * blockDim.x) {
         int c[4];
         site_coords(g, s, c);
-        for (int mu = mu0; mu <= mu1; ++mu) {
-            const int64_t smu = s + disp(g, mu, c[mu], 1);
+        int64_t sp[4];  // s + mu for every direction (compile-time indices only)
+#pragma unroll
+        for (int d = 0; d < 4; ++d) sp[d] = s + disp(g, d, c[d], 1);
+        // the six planes unrolled; the requested range selects them at run time
+#pragma unroll
+        for (int mu = 0; mu < 3; ++mu) {
+            if (mu < mu0 || mu > mu1) continue;
             const M3<T> umu = U.load(s, mu);
-            for (int nu = mu + 1; nu <= nu1; ++nu) {
-                const int64_t snu = s + disp(g, nu, c[nu], 1);
+#pragma unroll
+            for (int nu = mu + 1; nu < 4; ++nu) {
+                if (nu > nu1) continue;
                 // MultiplyMatdagMatdag(Umu_xnu, Unu_x) = Umu_xnu^+ Unu_x^+ = (Unu_x Umu_xnu)^+
-                const M3<T> a = mul(umu, U.load(smu, nu));
-                const M3<T> b = mul(U.load(s, nu), U.load(snu, mu));
+                const M3<T> a = mul(umu, U.load(sp[mu], nu));
+                const M3<T> b = mul(U.load(s, nu), U.load(sp[nu], mu));
                 acc += (double)retr_mm<false, true>(a, b);
             }
         }
