@@ -75,6 +75,7 @@ OBS_COST = {
     "plaquette (6 planes)": (4, 0, 6 * 2.2),
     "polyakov": (1, 0, 1.0),
     "wmunu 2x2 (1 plane)": (2, 0, 9.0),
+    "wmunu table R,T<=8 (1 plane)": (2, 0, 14.0 + 64 * 3),
     "genericpath 8 steps (every site)": (2, 1, 7.0),
     "clover F (1 plane)": (2, 1, 12.0 + 1),
     "5-loop F (1 plane)": (2, 1, 84.0 + 4),
@@ -106,6 +107,7 @@ def observables_bench(dims, steps):
             "plaquette (6 planes)": lambda: G.plaquette(f, 1, 4, 4),
             "polyakov": lambda: G.polyakov(f),
             "wmunu 2x2 (1 plane)": lambda: G.wmunu(f, 2, 3, 2, 2),
+            "wmunu table R,T<=8 (1 plane)": lambda: G.wmunu_table(f, 2, 3, 8, 8),
             "genericpath 8 steps (every site)": lambda: G.genericpath_all(f, path),
             "clover F (1 plane)": lambda: G.cloverloopmunucoord(f, 3, 2),
             "5-loop F (1 plane)": lambda: G.loop5munucoord(f, 3, 2),

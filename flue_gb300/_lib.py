@@ -91,6 +91,8 @@ SIGNATURES = {
     "flue_meanlink": ([_FP, _P, _I, _P, _P, _SZ, _P], _I),
     "flue_wflow_step": ([_FP, _D, _P, _SZ, _P], _I),
     "flue_gauge_transform": ([_FP, _P, _I, _P], _I),
+    "flue_wmunu_table_bytes": ([_I, _I, _I, _I, _I, _I, _I], _SZ),
+    "flue_wmunu_table": ([_FP, _I, _I, _I, _I, _P, _P, _SZ, _P], _I),
     "flue_gluon_propagator": ([_FP, _D, _I, _P, _P, _SZ, _P], _I),
     "flue_plaquette_c": ([_P, _I, _I, _I, _I, _I, _I, _I, _P, _P, _P], _I),
     "flue_genplaquette_c": ([_P, _I, _I, _I, _I, _I, _I, _I, _P, _P, _P], _I),

@@ -274,6 +274,28 @@ int flue_plaquette(const flue_field* U, int muStart, int muEnd, int nuEnd, doubl
     return cuda_status(launch_plaquette(F, muStart - 1, muEnd - 1, nuEnd - 1, (double*)ws, d_sum, (cudaStream_t)stream));
 }
 
+size_t flue_wmunu_table_bytes(int nt, int nx, int ny, int nz, int prec, int rmax, int tmax) {
+    if (!dims_ok(nt, nx, ny, nz) || !prec_ok(prec) || rmax < 1 || tmax < 1 || rmax > 64 || tmax > 64) return 0;
+    return wmunu_table_ws_bytes(make_geom(nt, nx, ny, nz), prec, rmax, tmax);
+}
+
+int flue_wmunu_table(const flue_field* U, int mu, int nu, int rmax, int tmax, double* d_out, void* ws,
+                     size_t ws_bytes, void* stream) {
+    FieldRef F;
+    int rc = check_field(U, &F);
+    if (rc) return rc;
+    if (!d_out) return fail(FLUE_ERR_ARG, "NULL output");
+    if (mu < 1 || mu > 4 || nu < 1 || nu > 4) return fail(FLUE_ERR_ARG, "direction out of 1..4");
+    if (rmax < 1 || tmax < 1 || rmax > 64 || tmax > 64) return fail(FLUE_ERR_ARG, "rmax, tmax must be 1..64");
+    const size_t need = wmunu_table_ws_bytes(F.g, F.prec, rmax, tmax);
+    if (!ws || ws_bytes < need) {
+        snprintf(g_detail, sizeof(g_detail), "workspace too small: need %zu bytes, got %zu", need, ws_bytes);
+        return FLUE_ERR_WORKSPACE;
+    }
+    if (((uintptr_t)ws) % 256) return fail(FLUE_ERR_LAYOUT, "workspace must be 256-byte aligned");
+    return cuda_status(launch_wmunu_table(F, mu - 1, nu - 1, rmax, tmax, d_out, ws, (cudaStream_t)stream));
+}
+
 int flue_polyakov(const flue_field* U, double* d_sum2, void* ws, size_t ws_bytes, void* stream) {
     FieldRef F;
     int rc = check_field(U, &F);

@@ -57,6 +57,9 @@ cudaError_t launch_wloop(const FieldRef& U, int tau, int mu, int nu, int nmu, in
                          cudaStream_t st);
 cudaError_t launch_genericpath(const FieldRef& U, const int* path_host, int npath, const int* coord_host, void* out,
                                cudaStream_t st);
+size_t wmunu_table_ws_bytes(const Geom& g, int prec, int rmax, int tmax);
+cudaError_t launch_wmunu_table(const FieldRef& U, int mu, int nu, int rmax, int tmax, double* out, void* ws,
+                               cudaStream_t st);
 int meanlink_blocks(const Geom& g);
 cudaError_t launch_meanlink(const FieldRef& U, const void* G, int g_dtype, double* part, double* out4, cudaStream_t st);
 

@@ -367,6 +367,100 @@ cudaError_t launch_wloop(const FieldRef& U, int tau, int mu, int nu, int nmu, in
 }
 
 // ---------------------------------------------------------------------------
+// W_munu table: wmunu(mu, nu, R, T) for every R <= rmax, T <= tmax at once
+// (the reference evaluates src/wloops.F90:679-791 once per (R, T), walking
+// every line anew).  k_wt_lines stores per site the mu-lines L_R = U_mu(x)
+// ... U_mu(x+(R-1)mu) and the nu-lines L_T, built incrementally; k_wt_loops
+// forms each loop from four stored lines, Re Tr[(A B)(D C)^+] with A = L_R(x),
+// B = L_T(x+R mu), C = L_R(x+T nu), D = L_T(x) -- the formula of k_wloop --
+// with the rmax * tmax tasks of one site block in adjacent blocks (the
+// neighbour lines they read stay in L2).
+// ---------------------------------------------------------------------------
+constexpr int WT_BS = 128;
+
+__device__ __forceinline__ void dir_of(const Geom& g, const int c[4], int d, int& cd, int& nd, int64_t& sd) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
+}
+
+template <class L, typename T>
+__global__ void k_wt_lines(L U, Geom g, int mu, int nu, int rmax, int tmax, MatAoS<T> lines) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.V) return;
+    int c[4];
+    site_coords(g, s, c);
+    for (int pass = 0; pass < 2; ++pass) {
+        const int d = pass ? nu : mu, n = pass ? tmax : rmax, k0 = pass ? rmax : 0;
+        int cd = 0, nd = 1;
+        int64_t sd = 1;
+        dir_of(g, c, d, cd, nd, sd);
+        int64_t sw = s;
+        M3<T> p = U.load(sw, d);
+        lines.store(s, k0, p);
+        for (int k = 1; k < n; ++k) {
+            sw += (cd + 1 == nd) ? -(int64_t)(nd - 1) * sd : sd;
+            cd = (cd + 1 == nd) ? 0 : cd + 1;
+            p = mul(p, U.load(sw, d));
+            lines.store(s, k0 + k, p);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(WT_BS) k_wt_loops(Geom g, int mu, int nu, int rmax, int tmax, MatAoS<T> lines,
+                                                    double* __restrict__ part) {
+    __shared__ double sh[32];
+    const int nrt = rmax * tmax;
+    const int rt = blockIdx.x % nrt;
+    const int sb = blockIdx.x / nrt;
+    const int nsb = gridDim.x / nrt;
+    const int R = rt / tmax + 1, Tl = rt % tmax + 1;
+    const int64_t s = (int64_t)sb * WT_BS + threadIdx.x;
+    double acc = 0.0;
+    if (s < g.V) {
+        int c[4];
+        site_coords(g, s, c);
+        int cm = 0, nm = 1, cn = 0, nn = 1;
+        int64_t sm = 1, sn = 1;
+        dir_of(g, c, mu, cm, nm, sm);
+        dir_of(g, c, nu, cn, nn, sn);
+        const int64_t sR = s + (int64_t)((cm + R) % nm - cm) * sm;
+        const int64_t sT = s + (int64_t)((cn + Tl) % nn - cn) * sn;
+        const M3<T> ab = mul(lines.load(s, R - 1), lines.load(sR, rmax + Tl - 1));
+        const M3<T> dc = mul(lines.load(s, rmax + Tl - 1), lines.load(sT, R - 1));
+        acc = (double)retr_mm<false, true>(ab, dc);
+    }
+    const double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[(int64_t)rt * nsb + sb] = r;
+}
+
+size_t wmunu_table_ws_bytes(const Geom& g, int prec, int rmax, int tmax) {
+    const size_t bpm = prec == PREC_C128 ? MatAoS<double>::bytes_per_matrix : MatAoS<float>::bytes_per_matrix;
+    const size_t nsb = (size_t)((g.V + WT_BS - 1) / WT_BS);
+    const size_t lines = (((size_t)(rmax + tmax) * g.V * bpm) + 255) & ~(size_t)255;
+    return lines + (((size_t)rmax * tmax * nsb * sizeof(double) + 255) & ~(size_t)255);
+}
+
+cudaError_t launch_wmunu_table(const FieldRef& U, int mu, int nu, int rmax, int tmax, double* out, void* ws,
+                               cudaStream_t st) {
+    const Geom& g = U.g;
+    const size_t bpm = U.prec == PREC_C128 ? MatAoS<double>::bytes_per_matrix : MatAoS<float>::bytes_per_matrix;
+    const size_t lines_b = (((size_t)(rmax + tmax) * g.V * bpm) + 255) & ~(size_t)255;
+    double* part = (double*)((char*)ws + lines_b);
+    const unsigned nsb = (unsigned)((g.V + WT_BS - 1) / WT_BS);
+    const unsigned nrt = (unsigned)(rmax * tmax);
+    FLUE_DISPATCH_LINKS(U, {
+        MatAoS<T> ln{reinterpret_cast<decltype(MatAoS<T>::p)>(ws), g.V};
+        note_launch(), k_wt_lines<decltype(L), T><<<nsb, WT_BS, 0, st>>>(L, g, mu, nu, rmax, tmax, ln);
+        note_launch(), k_wt_loops<T><<<nsb * nrt, WT_BS, 0, st>>>(g, mu, nu, rmax, tmax, ln, part);
+    });
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_finish_sums(part, (int)nsb, (int)nrt, out, st, 1.0 / (double)g.V);
+}
+
+// ---------------------------------------------------------------------------
 // genericPath (src/wloops.F90:20-57) at every site or one site.  Output is the
 // TRANSPOSE of the ordered product, in the layout (NT,NX,NY,NZ,3,3) (or one
 // 3x3 Fortran-ordered matrix), complex128 for FP64 fields, complex64 else.

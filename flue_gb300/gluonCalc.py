@@ -241,13 +241,17 @@ def wmunutau(data, tau, mu, nu, nmu, nnu, prec=None):
 
 def wmunu_table(data, mu, nu, rmax, tmax, prec=None):
     """All wmunu(data, mu, nu, R, T) for R in 1..rmax, T in 1..tmax as an
-    (rmax, tmax) array, queued on one stream with one host synchronisation."""
+    (rmax, tmax) array, from lines built once per site (flue_wmunu_table)."""
     f = as_field(data, prec)
+    L = _lib.load()
+    nt, nx, ny, nz = f.dims
+    nb = L.flue_wmunu_table_bytes(nt, nx, ny, nz, PRECS[f.prec], int(rmax), int(tmax))
+    ws = torch.empty(max(nb, 256), dtype=torch.uint8, device=f.device)
     out = torch.empty(rmax * tmax, dtype=torch.float64, device=f.device)
+    d = f.descriptor()
     with torch.cuda.device(f.device):
-        for r in range(rmax):
-            for t in range(tmax):
-                _wloop(f, 0, mu, nu, r + 1, t + 1, out, r * tmax + t)
+        _lib.call("flue_wmunu_table", ctypes.byref(d), int(mu), int(nu), int(rmax), int(tmax), _ptr(out), _ptr(ws),
+                  ws.numel(), _stream_handle())
     return np.asarray(_scalars(out)).reshape(rmax, tmax)
 
 

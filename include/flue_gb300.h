@@ -146,6 +146,13 @@ int flue_plaquette(const flue_field *U, int muStart, int muEnd, int nuEnd, doubl
 /* polyakov (src/wloops.F90:1019-1069): d_sum[0] = sum_x Re Tr prod_t U_1,
  * d_sum[1] = the imaginary part.  nP = NX*NY*NZ. */
 int flue_polyakov(const flue_field *U, double *d_sum2, void *ws, size_t ws_bytes, void *stream);
+/* The W_munu table: d_out[(R-1)*tmax + (T-1)] = wmunu(mu, nu, R, T)
+ * (src/wloops.F90:679-791, whole lattice, normalised by V) for every
+ * R <= rmax, T <= tmax (1..64), from lines built once per site instead of
+ * one call per (R, T); scratch flue_wmunu_table_bytes(...) bytes. */
+size_t flue_wmunu_table_bytes(int nt, int nx, int ny, int nz, int prec, int rmax, int tmax);
+int flue_wmunu_table(const flue_field *U, int mu, int nu, int rmax, int tmax, double *d_out, void *ws,
+                     size_t ws_bytes, void *stream);
 /* wmunu (src/wloops.F90:679-791) for tau = 0, wmunutau (:567-677) for
  * tau in 1..NT: d_val[0] = the MEAN nMu x nNu loop (divided by V or NX*NY*NZ). */
 int flue_wmunu(const flue_field *U, int tau, int mu, int nu, int nMu, int nNu, double *d_val, void *ws,

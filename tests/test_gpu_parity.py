@@ -226,3 +226,21 @@ def test_kernel_launch_counter():
     n0 = L.flue_kernel_launches()
     G.plaquette(f, 1, 4, 4)
     assert L.flue_kernel_launches() - n0 == 2
+
+
+@pytest.mark.parametrize("dims,mu,nu,rmax,tmax", [((6, 4, 5, 3), 2, 3, 8, 8), ((5, 3, 4, 6), 1, 4, 7, 9),
+                                                  ((4, 4, 4, 4), 4, 2, 5, 3)])
+def test_wmunu_table_vs_single_loops(dims, mu, nu, rmax, tmax):
+    """The table entry (lines built once per site) against one wmunu call
+    per (R, T) and the oracle, R and T up to and past the extents (the walk
+    wraps), FP64 to 1e-12; FP32 against FP64 to 1e-5."""
+    U = generate.random_field(dims, 0.4, 31)
+    tab = G.wmunu_table(U, mu, nu, rmax, tmax)
+    for r in range(rmax):
+        for t in range(tmax):
+            single = G.wmunu(U, mu, nu, r + 1, t + 1)
+            assert abs(tab[r, t] - single) < 1e-12 * max(1.0, abs(single))
+    for r, t in ((0, 0), (rmax - 1, tmax - 1), (rmax // 2, 1)):
+        assert abs(tab[r, t] - oracle.wmunu(U, mu, nu, r + 1, t + 1)) < 1e-12
+    tab32 = G.wmunu_table(GaugeField.from_array(U, prec="r12"), mu, nu, rmax, tmax)
+    assert np.abs(tab32 - tab).max() < 1e-5
