@@ -1,0 +1,48 @@
+"""Smallest lattices: extents of 1 and 2 (every stencil wraps onto itself,
+through the general wrap path) for B^2 and its gradient, the 5-loop F, the
+plaquette ranges, the Polyakov loop, the W_munu table and the gluon
+propagator, against the oracles in FP64."""
+import numpy as np
+import pytest
+
+import oracle
+from flue_gb300 import forces, generate, gluonCalc as G, gluonProp
+from oracle import propagator as P
+
+pytestmark = pytest.mark.gpu
+
+DIMS = [(3, 1, 2, 2), (4, 2, 1, 3), (2, 3, 2, 1), (1, 2, 2, 2)]
+
+
+@pytest.fixture(scope="module", params=range(len(DIMS)))
+def U(request):
+    return generate.random_field(DIMS[request.param], 0.6, 40 + request.param)
+
+
+def test_b2_force_small_extents(U):
+    b, g = forces.magnetic_force(U)
+    assert abs(b - oracle.magnetic(U)) < 1e-12 * max(1.0, abs(b))
+    go = oracle.loop5_energy_force(U, oracle.B2_PLANES)
+    gn = g.detach().cpu().numpy() if hasattr(g, "detach") else g
+    assert np.abs(gn - go).max() < 1e-11 * max(1.0, np.abs(go).max())
+
+
+def test_fmunu_and_plaquettes_small_extents(U):
+    for mu, nu in ((3, 2), (1, 4)):
+        assert np.abs(G.loop5munucoord(U, mu, nu) - oracle.loop5munucoord(U, mu, nu)).max() < 1e-12
+    for rng in ((1, 4, 4), (2, 4, 4), (1, 1, 4)):
+        s, n, _ = G.plaquette(U, *rng)
+        so, no = oracle.plaquette(U, *rng)
+        assert n == no and abs(s - so) < 1e-12 * max(1.0, abs(so))
+    if U.shape[0] >= 3:
+        assert abs(G.polyakov(U)[0] - oracle.polyakov(U)[0]) < 1e-12 * U[0, ..., 0, 0, 0].size
+
+
+def test_wmunu_table_and_propagator_small_extents(U):
+    tab = G.wmunu_table(U, 2, 4, 3, 3)
+    for r in range(3):
+        for t in range(3):
+            assert abs(tab[r, t] - oracle.wmunu(U, 2, 4, r + 1, t + 1)) < 1e-12
+    D = gluonProp.scalar_gluon_prop(U, 1.4, 0)
+    Dr = P.gluon_propagator(U, 1.4, 0)
+    assert np.abs(D - Dr).max() < 1e-12 * np.abs(Dr).max()
