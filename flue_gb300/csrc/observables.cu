@@ -313,16 +313,23 @@ cudaError_t launch_polyakov(const FieldRef& U, double* part, double* out2, cudaS
 // ---------------------------------------------------------------------------
 int wloop_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
 
+// coordinate, extent and stride of direction d (runtime) without
+// runtime-indexed arrays (they would go to local memory)
+__device__ __forceinline__ void dir_of(const Geom& g, const int c[4], int d, int& cd, int& nd, int64_t& sd) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
+}
+
+// product U_d(x) U_d(x+d) ... of n links starting at site s, whose
+// coordinate along d is cd (extent nd, stride sd)
 template <class L, typename T>
-__device__ __forceinline__ M3<T> line_walk(const L& U, const Geom& g, int64_t s, const int c[4], int mu, int n) {
-    // product U_mu(x) U_mu(x+mu) ... of n links starting at site s (coords c)
-    M3<T> p = U.load(s, mu);
-    int cm = c[mu];
+__device__ __forceinline__ M3<T> line_walk(const L& U, int64_t s, int d, int cd, int nd, int64_t sd, int n) {
+    M3<T> p = U.load(s, d);
     for (int k = 1; k < n; ++k) {
-        const int64_t d = disp(g, mu, cm, 1);
-        s += d;
-        cm = (cm + 1 == g.n[mu]) ? 0 : cm + 1;
-        p = mul(p, U.load(s, mu));
+        s += (cd + 1 == nd) ? -(int64_t)(nd - 1) * sd : sd;
+        cd = (cd + 1 == nd) ? 0 : cd + 1;
+        p = mul(p, U.load(s, d));
     }
     return p;
 }
@@ -337,16 +344,16 @@ __global__ void __launch_bounds__(RED_BS)
         const int64_t s = tau < 0 ? j : (int64_t)tau + j * g.n[0];
         int c[4];
         site_coords(g, s, c);
-        const M3<T> a = line_walk<L, T>(U, g, s, c, mu, nmu);
-        int c2[4] = {c[0], c[1], c[2], c[3]};
-        const int64_t dmu = disp(g, mu, c[mu], nmu);
-        c2[mu] = (int)(((int64_t)c[mu] + nmu) % g.n[mu]);
-        const M3<T> b = line_walk<L, T>(U, g, s + dmu, c2, nu, nnu);
-        int c3[4] = {c[0], c[1], c[2], c[3]};
-        const int64_t dnu = disp(g, nu, c[nu], nnu);
-        c3[nu] = (int)(((int64_t)c[nu] + nnu) % g.n[nu]);
-        const M3<T> cc = line_walk<L, T>(U, g, s + dnu, c3, mu, nmu);
-        const M3<T> d = line_walk<L, T>(U, g, s, c, nu, nnu);
+        int cm = 0, nm = 1, cn = 0, nn = 1;
+        int64_t sm = 1, sn = 1;
+        dir_of(g, c, mu, cm, nm, sm);
+        dir_of(g, c, nu, cn, nn, sn);
+        const int cm2 = (int)(((int64_t)cm + nmu) % nm), cn2 = (int)(((int64_t)cn + nnu) % nn);
+        const int64_t smu = s + (int64_t)(cm2 - cm) * sm, snu = s + (int64_t)(cn2 - cn) * sn;
+        const M3<T> a = line_walk<L, T>(U, s, mu, cm, nm, sm, nmu);
+        const M3<T> b = line_walk<L, T>(U, smu, nu, cn, nn, sn, nnu);   // x + nMu mu: same nu coordinate
+        const M3<T> cc = line_walk<L, T>(U, snu, mu, cm, nm, sm, nmu);  // x + nNu nu: same mu coordinate
+        const M3<T> d = line_walk<L, T>(U, s, nu, cn, nn, sn, nnu);
         // Re Tr[(A B) (C^+ D^+)] with C^+ D^+ = (D C)^+  (MultiplyMatdagMatdag, :669)
         const M3<T> ab = mul(a, b);
         const M3<T> dc = mul(d, cc);
@@ -377,12 +384,6 @@ cudaError_t launch_wloop(const FieldRef& U, int tau, int mu, int nu, int nmu, in
 // neighbour lines they read stay in L2).
 // ---------------------------------------------------------------------------
 constexpr int WT_BS = 128;
-
-__device__ __forceinline__ void dir_of(const Geom& g, const int c[4], int d, int& cd, int& nd, int64_t& sd) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
-}
 
 template <class L, typename T>
 __global__ void k_wt_lines(L U, Geom g, int mu, int nu, int rmax, int tmax, MatAoS<T> lines) {
@@ -481,18 +482,31 @@ __global__ void k_genericpath(L U, Geom g, PathArg path, int64_t s_single, typen
     site_coords(g, s0, c);
     int64_t s = s0;
     M3<T> p = m_ident<T>();
+    // one periodic step of +-1 along direction mu (runtime); the branch over
+    // the four directions keeps coordinates and strides in registers
+    auto move = [&](int mu, int dir) {
+#pragma unroll
+        for (int d = 0; d < 4; ++d)
+            if (d == mu) {
+                const int n = g.n[d];
+                int cd = c[d] + dir;
+                int64_t ds = dir * g.st[d];
+                if (cd < 0) cd += n, ds += (int64_t)n * g.st[d];
+                if (cd >= n) cd -= n, ds -= (int64_t)n * g.st[d];
+                c[d] = cd;
+                s += ds;
+            }
+    };
     for (int k = 0; k < path.n; ++k) {
         const int st = path.step[k];
         if (st < 0) {
             const int mu = -st - 1;
-            s += disp(g, mu, c[mu], -1);
-            c[mu] = c[mu] == 0 ? g.n[mu] - 1 : c[mu] - 1;
+            move(mu, -1);
             p = mm<false, true>(p, U.load(s, mu));
         } else {
             const int mu = st - 1;
             p = mul(p, U.load(s, mu));
-            s += disp(g, mu, c[mu], 1);
-            c[mu] = (c[mu] + 1 == g.n[mu]) ? 0 : c[mu] + 1;
+            move(mu, 1);
         }
     }
     RefOut<T> o{out, single ? 1 : g.V, 1};

@@ -64,8 +64,12 @@ __global__ void k_gauge_transform(L U, void* links, int prec, Geom g, const G2* 
     const int mu = (int)(idx / g.V);
     int c[4];
     site_coords(g, s, c);
+    int64_t sp = s;  // x + mu, selected without runtime-indexed arrays
+#pragma unroll
+    for (int d = 0; d < 4; ++d)
+        if (d == mu) sp = s + (c[d] + 1 == g.n[d] ? -(int64_t)(g.n[d] - 1) * g.st[d] : g.st[d]);
     const M3<T> gx = load_gt<T>(G, g.V, s);
-    const M3<T> gp = load_gt<T>(G, g.V, s + disp(g, mu, c[mu], 1));
+    const M3<T> gp = load_gt<T>(G, g.V, sp);
     const M3<T> w = mm<false, true>(mul(gx, U.load(s, mu)), gp);
     if (prec == PREC_R12) {
         float4* o = (float4*)links + s + g.V * (3 * mu);
