@@ -41,13 +41,16 @@ def _ptr(t: torch.Tensor):
 
 
 class Workspace:
-    """Per-device scratch buffers reused across calls (allocated by torch)."""
+    """Scratch buffers reused across calls (allocated by torch), one per
+    (device, stream): calls queued on the same stream run in order and can
+    share one, calls on different streams may run at once and must not."""
 
     _bufs = {}
 
     @classmethod
     def get(cls, nbytes: int, device) -> torch.Tensor:
-        key = torch.device(device).index or 0
+        dev = torch.device(device)
+        key = (dev.index or 0, torch.cuda.current_stream(dev).cuda_stream)
         buf = cls._bufs.get(key)
         if buf is None or buf.numel() < nbytes:
             buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)

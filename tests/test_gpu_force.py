@@ -222,3 +222,39 @@ def test_host_buffer_force_staged_copies(copy_streams, monkeypatch):
     L.flue_release_host_cache()
     assert abs(b_st - b_zc) < 1e-12 * abs(b_zc)
     assert torch.equal(g_st, g_zc)
+
+
+def test_concurrent_host_threads(monkeypatch):
+    """Four host threads computing B^2 forces of different fields at once (the
+    time-slab path shares the library's streams and events between calls)
+    get the same results as one thread in turn."""
+    import threading
+
+    monkeypatch.setenv("FLUE_SLABS", "4")
+    Us = [generate.random_field((8, 4, 6, 4), 0.4, 60 + k) for k in range(4)]
+    fs = [GaugeField.from_array(U, prec="r12") for U in Us]
+    seq = [forces.magnetic_force(f) for f in fs]
+    seq = [(b, _np(g).copy()) for b, g in seq]
+    out = [None] * 4
+    errs = []
+
+    def work(k):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                b, g = forces.magnetic_force(fs[k])
+                s.synchronize()
+                out[k] = (b, _np(g).copy())
+        except Exception as e:  # pragma: no cover - reported below
+            errs.append(e)
+
+    for _ in range(3):
+        th = [threading.Thread(target=work, args=(k,)) for k in range(4)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        assert not errs, errs
+        for (b, g), (bs, gs) in zip(out, seq):
+            assert abs(b - bs) < 1e-12 * abs(bs)
+            assert np.array_equal(g, gs)
