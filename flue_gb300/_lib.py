@@ -71,6 +71,7 @@ SIGNATURES = {
     "flue_abi_version": ([], _I),
     "flue_stage_timing": ([_I], _I),
     "flue_kernel_launches": ([], ctypes.c_uint64),
+    "flue_bounds_errors": ([], ctypes.c_int64),
     "flue_stage_times": ([_P, _I, _P], _I),
     "flue_field_bytes": ([_I, _I, _I, _I, _I], _I64),
     "flue_workspace_bytes": ([_I, _I, _I, _I, _I, _I], _SZ),

@@ -207,6 +207,15 @@ int flue_stage_timing(int enable) { return cuda_status(stage_timing_enable(enabl
 
 uint64_t flue_kernel_launches(void) { return (uint64_t)g_launches.load(std::memory_order_relaxed); }
 
+int64_t flue_bounds_errors(void) {
+    if (!FLUE_BOUNDS_CHECK) return -1;
+    const unsigned c[] = {oob_capi(), oob_ensemble(), oob_flow(), oob_force(), oob_noalloc(), oob_observables(),
+                          oob_propagator()};
+    int64_t n = 0;
+    for (unsigned v : c) n += v == 0xffffffffu ? 0 : v;
+    return n;
+}
+
 int flue_stage_times(double* ms, int max_stages, int* n_stages) {
     if (!ms || !n_stages || max_stages < 0) return fail(FLUE_ERR_ARG, "NULL pointer");
     return cuda_status(stage_times(ms, max_stages, n_stages));
@@ -1022,3 +1031,7 @@ void flue_release_host_cache(void) {
 }
 
 }  // extern "C"
+
+namespace flue {
+FLUE_OOB_READER(capi)
+}  // namespace flue

@@ -233,6 +233,8 @@ __global__ void k_ensemble_finish(const double* __restrict__ part, const int* __
     out[f * NOBS + o] = acc;
 }
 
+FLUE_OOB_READER(ensemble)
+
 }  // namespace flue
 
 // ===========================================================================

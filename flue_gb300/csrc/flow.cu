@@ -135,6 +135,7 @@ __device__ __forceinline__ M3<T> expm1_m3(const M3<T>& x) {
 template <typename T>
 __device__ __forceinline__ M3<T> load_full(const void* links, int64_t V, int64_t s, int mu) {
     using C2 = typename V2<T>::type;
+    if (!FLUE_INB(s >= 0 && s < V && mu >= 0 && mu < 4)) return m_zero<T>();
     const C2* q = (const C2*)links + s + V * mu;
     M3<T> m;
 #pragma unroll
@@ -312,5 +313,7 @@ cudaError_t launch_wflow_step(void* links, const Geom& g, int prec, double eps, 
     }
     return cudaSuccess;
 }
+
+FLUE_OOB_READER(flow)
 
 }  // namespace flue

@@ -24,7 +24,39 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// Bounds-checked build (-DFLUE_BOUNDS_CHECK=1): the link and intermediate
+// accessors check every index, count violations in a device counter of the
+// translation unit and skip the access (loads return zeros) -- no trap, no
+// fault.  flue_bounds_errors() reads and clears the counters.  Off by default.
+#ifndef FLUE_BOUNDS_CHECK
+#define FLUE_BOUNDS_CHECK 0
+#endif
+
 namespace flue {
+
+#if FLUE_BOUNDS_CHECK
+namespace {
+__device__ unsigned int g_oob_count;  // one per translation unit
+}
+__device__ __forceinline__ bool in_bounds(bool ok) {
+    if (!ok) atomicAdd(&g_oob_count, 1u);
+    return ok;
+}
+// read and clear this translation unit's counter (host)
+static inline unsigned oob_read_clear() {
+    unsigned v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, g_oob_count, sizeof(v)) != cudaSuccess) return 0xffffffffu;
+    cudaMemcpyToSymbol(g_oob_count, &z, sizeof(z));
+    return v;
+}
+#define FLUE_INB(cond) ::flue::in_bounds(cond)
+#else
+static inline unsigned oob_read_clear() { return 0; }
+#define FLUE_INB(cond) true
+#endif
+// per translation unit: unsigned flue::oob_<name>() for flue_bounds_errors()
+#define FLUE_OOB_READER(name) \
+    unsigned oob_##name() { return oob_read_clear(); }
 
 enum Prec : int { PREC_C128 = 0, PREC_C64 = 1, PREC_R12 = 2 };
 
@@ -316,6 +348,7 @@ struct FullLinks {
     int64_t V;
     __device__ __forceinline__ M3<T> load(int64_t s, int mu) const {
         M3<T> m;
+        if (!FLUE_INB(s >= 0 && s < V && mu >= 0 && mu < 4)) return m_zero<T>();
         const C2* q = p + s + V * mu;
         const int64_t st = 4 * V;
 #pragma unroll
@@ -348,6 +381,7 @@ struct R12Links {
     int64_t V;
     __device__ __forceinline__ M3<float> load(int64_t s, int mu) const {
         M3<float> m;
+        if (!FLUE_INB(s >= 0 && s < V && mu >= 0 && mu < 4)) return m_zero<float>();
         const float4* q = p + s + V * (3 * mu);
         const float4 a = __ldg(q), b = __ldg(q + V), c = __ldg(q + 2 * V);
         m.r[0] = a.x;
@@ -376,6 +410,7 @@ struct MatPlanes {
     int64_t V;
     __device__ __forceinline__ M3<T> load(int64_t s, int k) const {
         M3<T> m;
+        if (!FLUE_INB(s >= 0 && s < V && k >= 0)) return m_zero<T>();
         const C2* q = p + (int64_t)k * 9 * V + s;
 #pragma unroll
         for (int e = 0; e < 9; ++e) {
@@ -386,6 +421,7 @@ struct MatPlanes {
         return m;
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<T>& m) const {
+        if (!FLUE_INB(s >= 0 && s < V && k >= 0)) return;
         C2* q = p + (int64_t)k * 9 * V + s;
 #pragma unroll
         for (int e = 0; e < 9; ++e) {
@@ -408,7 +444,12 @@ template <>
 struct MatAoS<float> {
     float4* __restrict__ p;
     int64_t V;
+    int nk = 0;  // planes, checked when > 0 (bounds-checked build)
+    __device__ __forceinline__ bool ok(int64_t s, int k) const {
+        return FLUE_INB(s >= 0 && s < V && k >= 0 && (nk == 0 || k < nk));
+    }
     __device__ __forceinline__ M3<float> load(int64_t s, int k) const {
+        if (!ok(s, k)) return m_zero<float>();
         const float4* q = p + ((int64_t)k * V + s) * 5;
         M3<float> m;
 #pragma unroll
@@ -425,6 +466,7 @@ struct MatAoS<float> {
         return m;
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<float>& m) const {
+        if (!ok(s, k)) return;
         float4* q = p + ((int64_t)k * V + s) * 5;
 #pragma unroll
         for (int j = 0; j < 4; ++j) q[j] = make_float4(m.r[2 * j], m.i[2 * j], m.r[2 * j + 1], m.i[2 * j + 1]);
@@ -437,7 +479,12 @@ template <>
 struct MatAoS<double> {
     double2* __restrict__ p;
     int64_t V;
+    int nk = 0;  // planes, checked when > 0 (bounds-checked build)
+    __device__ __forceinline__ bool ok(int64_t s, int k) const {
+        return FLUE_INB(s >= 0 && s < V && k >= 0 && (nk == 0 || k < nk));
+    }
     __device__ __forceinline__ M3<double> load(int64_t s, int k) const {
+        if (!ok(s, k)) return m_zero<double>();
         const double2* q = p + ((int64_t)k * V + s) * 9;
         M3<double> m;
 #pragma unroll
@@ -449,6 +496,7 @@ struct MatAoS<double> {
         return m;
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<double>& m) const {
+        if (!ok(s, k)) return;
         double2* q = p + ((int64_t)k * V + s) * 9;
 #pragma unroll
         for (int e = 0; e < 9; ++e) q[e] = make_double2(m.r[e], m.i[e]);
@@ -553,7 +601,15 @@ template <>
 struct AHAoS<float> {
     float4* __restrict__ p;
     int64_t V;
+    int nk = 0;  // planes, checked when > 0 (bounds-checked build)
+    __device__ __forceinline__ bool ok(int64_t s, int k) const {
+        return FLUE_INB(s >= 0 && s < V && k >= 0 && (nk == 0 || k < nk));
+    }
     __device__ __forceinline__ void load_packed(int64_t s, int k, float v[9]) const {
+        if (!ok(s, k)) {
+            for (int e = 0; e < 9; ++e) v[e] = 0;
+            return;
+        }
         const float4* q = p + ((int64_t)k * V + s) * 3;
         const float4 a = q[0], b = q[1], c = q[2];
         v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w;
@@ -561,12 +617,14 @@ struct AHAoS<float> {
         v[8] = c.x;
     }
     __device__ __forceinline__ M3<float> load(int64_t s, int k) const {
+        if (!ok(s, k)) return m_zero<float>();
         const float4* q = p + ((int64_t)k * V + s) * 3;
         const float4 a = q[0], b = q[1], c = q[2];
         const float v[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
         return ah_expand<float>(v);
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<float>& m) const {
+        if (!ok(s, k)) return;
         float4* q = p + ((int64_t)k * V + s) * 3;
         q[0] = make_float4(m.i[0], m.i[4], m.i[8], m.r[1]);
         q[1] = make_float4(m.i[1], m.r[2], m.i[2], m.r[5]);
@@ -579,19 +637,29 @@ template <>
 struct AHAoS<double> {
     double2* __restrict__ p;
     int64_t V;
+    int nk = 0;  // planes, checked when > 0 (bounds-checked build)
+    __device__ __forceinline__ bool ok(int64_t s, int k) const {
+        return FLUE_INB(s >= 0 && s < V && k >= 0 && (nk == 0 || k < nk));
+    }
     __device__ __forceinline__ void load_packed(int64_t s, int k, double v[9]) const {
+        if (!ok(s, k)) {
+            for (int e = 0; e < 9; ++e) v[e] = 0;
+            return;
+        }
         const double2* q = p + ((int64_t)k * V + s) * 5;
         const double2 a = q[0], b = q[1], c = q[2], d = q[3], e = q[4];
         v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y, v[4] = c.x;
         v[5] = c.y, v[6] = d.x, v[7] = d.y, v[8] = e.x;
     }
     __device__ __forceinline__ M3<double> load(int64_t s, int k) const {
+        if (!ok(s, k)) return m_zero<double>();
         const double2* q = p + ((int64_t)k * V + s) * 5;
         const double2 a = q[0], b = q[1], c = q[2], d = q[3], e = q[4];
         const double v[9] = {a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x};
         return ah_expand<double>(v);
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<double>& m) const {
+        if (!ok(s, k)) return;
         double2* q = p + ((int64_t)k * V + s) * 5;
         q[0] = make_double2(m.i[0], m.i[4]);
         q[1] = make_double2(m.i[8], m.r[1]);
@@ -610,6 +678,7 @@ struct AHPlanes {
     T* __restrict__ p;
     int64_t V;
     __device__ __forceinline__ M3<T> load(int64_t s, int k) const {
+        if (!FLUE_INB(s >= 0 && s < V && k >= 0)) return m_zero<T>();
         const T* q = p + (int64_t)k * 9 * V + s;
         T v[9];
 #pragma unroll
@@ -634,6 +703,7 @@ struct AHPlanes {
         return m;
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<T>& m) const {
+        if (!FLUE_INB(s >= 0 && s < V && k >= 0)) return;
         T* q = p + (int64_t)k * 9 * V + s;
         q[0] = m.i[0];
         q[V] = m.i[4];
@@ -661,6 +731,7 @@ struct RefOut {
     int nts = 0, ntf = 0, t0 = 0;
     __device__ __forceinline__ void store(int64_t s, int slot, const M3<T>& m) const {
         const int64_t sf = nts ? (int64_t)t0 + s % nts + (int64_t)ntf * (s / nts) : s;
+        if (!FLUE_INB(sf >= 0 && sf < V && slot >= 0 && slot < nslot)) return;
         C2* q = p + sf + V * slot;
         const int64_t st = V * nslot;
 #pragma unroll

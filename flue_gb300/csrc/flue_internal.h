@@ -97,6 +97,16 @@ int plaqforce_blocks(const Geom& g);
 cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_S, void* force, int force_form,
                                    cudaStream_t st);
 
+// out-of-bounds counters of the bounds-checked build, one per translation
+// unit (read and cleared; 0 in the normal build)
+unsigned oob_capi();
+unsigned oob_ensemble();
+unsigned oob_flow();
+unsigned oob_force();
+unsigned oob_noalloc();
+unsigned oob_observables();
+unsigned oob_propagator();
+
 // text returned by flue_last_error_detail() on the calling thread
 void set_error_detail(const char* msg);
 

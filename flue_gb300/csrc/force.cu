@@ -915,4 +915,6 @@ cudaError_t launch_plaquette_force(const FieldRef& U, double* part, double* out_
     return launch_finish_sums(part, 4 * nb, 1, out_S, st);
 }
 
+FLUE_OOB_READER(force)
+
 }  // namespace flue

@@ -93,3 +93,7 @@ extern "C" int flue_plaquette_noalloc(const flue_field* U, int muStart, int muEn
     cudaError_t e = flue::launch_plaquette(F, muStart - 1, muEnd - 1, nuEnd - 1, scratch, d_sum, (cudaStream_t)stream);
     return e == cudaSuccess ? FLUE_OK : FLUE_ERR_CUDA;
 }
+
+namespace flue {
+FLUE_OOB_READER(noalloc)
+}  // namespace flue

@@ -582,6 +582,7 @@ int meanlink_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
 template <typename T, typename G2>
 __device__ __forceinline__ M3<T> load_g(const G2* __restrict__ G, int64_t V, int64_t s) {
     M3<T> m;
+    if (!FLUE_INB(s >= 0 && s < V)) return m_zero<T>();
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -627,5 +628,7 @@ cudaError_t launch_meanlink(const FieldRef& U, const void* G, int g_dtype, doubl
     if (e != cudaSuccess) return e;
     return launch_finish_sums(part, nb, 4, out4, st);
 }
+
+FLUE_OOB_READER(observables)
 
 }  // namespace flue

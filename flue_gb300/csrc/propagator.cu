@@ -45,6 +45,7 @@ namespace flue {
 template <typename T, typename G2>
 __device__ __forceinline__ M3<T> load_gt(const G2* __restrict__ G, int64_t V, int64_t s) {
     M3<T> m;
+    if (!FLUE_INB(s >= 0 && s < V)) return m_zero<T>();
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -120,6 +121,7 @@ __global__ void k_colour_fields(L U, Geom g, int cmajor, T* __restrict__ a) {
     const M3<T> u = U.load(s, mu);
     const int64_t nt = g.n[0];
     const int64_t t = s % nt, s3 = s / nt;
+    if (!FLUE_INB(s >= 0 && s < g.V && mu >= 0 && mu < 4)) return;  // 32 V outputs
     // component-major a[(c * V3 + s3) * NT + t], or site-major a[(s3 * 32 + c) * NT + t]
     const int64_t cs = cmajor ? g.V : nt;
     T* o = cmajor ? a + (8 * mu) * cs + s3 * nt + t : a + (s3 * 32 + 8 * mu) * nt + t;
@@ -153,6 +155,7 @@ __global__ void k_prop_sum(const typename V2<T>::type* __restrict__ F, Geom g, i
     const typename V2<T>::type* f = cmajor ? F + kt * v3 + s3 : F + s3 * 32 * nth + kt;
     const int64_t fs = cmajor ? (int64_t)nth * v3 : nth;  // component stride
     double sum = 0.0;
+    if (!FLUE_INB(s3 >= 0 && s3 < v3 && kt >= 0 && kt < nth)) return;  // F holds 32 * v3 * nth
     for (int mu = mu_start; mu < 4; ++mu) {
         double s = 0.0;
 #pragma unroll
@@ -337,5 +340,7 @@ cudaError_t launch_gluon_propagator(const FieldRef& U, double xi, int mu_start, 
                            <<<nq, 128, 0, st>>>((const float2*)(base + w.spec), g, nth, (int)prop_cmajor(false), xi * xi, mu_start, D);
     return cudaGetLastError();
 }
+
+FLUE_OOB_READER(propagator)
 
 }  // namespace flue

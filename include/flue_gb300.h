@@ -112,6 +112,10 @@ int flue_stage_times(double *ms, int max_stages, int *n_stages);
  * devices; a replayed ensemble graph counts its two kernels).  For launch
  * accounting by benchmarks and tests; no reference counterpart. */
 uint64_t flue_kernel_launches(void);
+/* Bounds-checked build only (compiled with -DFLUE_BOUNDS_CHECK=1): the number
+ * of out-of-range indices the kernels' accessors met (and skipped) since the
+ * last call; -1 in a normal build.  No reference counterpart. */
+int64_t flue_bounds_errors(void);
 
 /* ======================================================================== */
 /* Tier 2: device entry points                                              */
