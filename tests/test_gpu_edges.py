@@ -46,3 +46,21 @@ def test_wmunu_table_and_propagator_small_extents(U):
     D = gluonProp.scalar_gluon_prop(U, 1.4, 0)
     Dr = P.gluon_propagator(U, 1.4, 0)
     assert np.abs(D - Dr).max() < 1e-12 * np.abs(Dr).max()
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64", "r12"])
+def test_nan_links_propagate_and_leave_the_library_usable(prec):
+    """A NaN link makes B^2, the plaquette and the nearby gradient NaN (no
+    call fails); the next calls on a clean field give the clean results."""
+    from flue_gb300.field import GaugeField
+
+    U = generate.random_field((4, 4, 4, 4), 0.4, 50)
+    clean = forces.magnetic_force(GaugeField.from_array(U, prec=prec))[0]
+    bad = U.copy()
+    bad[1, 2, 0, 3, 2, 0, 1] = np.nan
+    b, g = forces.magnetic_force(GaugeField.from_array(bad, prec=prec))
+    gn = g.detach().cpu().numpy()
+    assert np.isnan(b) and np.isnan(gn).any() and np.isfinite(gn).any()
+    assert np.isnan(G.plaquette(GaugeField.from_array(bad, prec=prec), 1, 4, 4)[0])
+    again = forces.magnetic_force(GaugeField.from_array(U, prec=prec))[0]
+    assert again == clean
