@@ -7,6 +7,7 @@ advances by ``eps`` per step.  No reference counterpart.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import torch
 
@@ -24,10 +25,17 @@ def wflow_step(field: GaugeField, eps: float) -> GaugeField:
 
 
 def wilson_flow(data, eps: float = 0.01, tmax: float = 2.0, measure_every: float = 0.1, prec=None,
-                observables=("b2", "plaq")):
+                observables=("b2", "plaq"), checkpoint=None):
     """Flow ``data`` to t = tmax with step eps; every ``measure_every`` in
     flow time (and at t = 0) record t, B^2 and the mean plaquette
-    <Re Tr P>/3.  Returns (flowed GaugeField, list of dict records)."""
+    <Re Tr P>/3.  Returns (flowed GaugeField, list of dict records).
+
+    ``checkpoint``: a file path.  After every measurement the step count,
+    the records and the links are saved there (torch.save, written to a
+    temporary name and renamed, so an interrupted save leaves the previous
+    checkpoint); a call whose checkpoint file exists, for the same lattice,
+    precision and eps, continues from it instead of from ``data``.  The
+    continued flow is bitwise the uninterrupted one."""
     f = as_field(data, prec)
     if f.prec == "r12":
         raise ValueError("the Wilson flow updates links in place; use a c128 or c64 field")
@@ -35,6 +43,14 @@ def wilson_flow(data, eps: float = 0.01, tmax: float = 2.0, measure_every: float
     nsteps = int(round(tmax / eps))
     every = max(1, int(round(measure_every / eps)))
     recs = []
+    start = 1
+    if checkpoint is not None and os.path.exists(checkpoint):
+        ck = torch.load(checkpoint, map_location="cpu", weights_only=False)
+        if tuple(ck["dims"]) != tuple(f.dims) or ck["prec"] != f.prec or ck["eps"] != eps:
+            raise ValueError("checkpoint %s is for another lattice, precision or step" % checkpoint)
+        f.storage.copy_(ck["links"].to(f.device))
+        recs = list(ck["recs"])
+        start = ck["step"] + 1
 
     def measure(step):
         r = {"t": step * eps}
@@ -44,9 +60,15 @@ def wilson_flow(data, eps: float = 0.01, tmax: float = 2.0, measure_every: float
             s, n, _ = gluonCalc.plaquette(f, 1, 4, 4)
             r["plaq"] = s / n / 3.0
         recs.append(r)
+        if checkpoint is not None:
+            tmp = checkpoint + ".tmp"
+            torch.save({"dims": f.dims, "prec": f.prec, "eps": eps, "step": step, "recs": recs,
+                        "links": f.storage.detach().cpu()}, tmp)
+            os.replace(tmp, checkpoint)
 
-    measure(0)
-    for k in range(1, nsteps + 1):
+    if start == 1:
+        measure(0)
+    for k in range(start, nsteps + 1):
         wflow_step(f, eps)
         if k % every == 0:
             measure(k)

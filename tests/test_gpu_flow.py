@@ -67,3 +67,17 @@ def test_fp32_flow_no_drift():
     for a, b in zip(r64, r32):
         assert abs(a["b2"] - b["b2"]) / a["b2"] < 1e-6, (a, b)
         assert abs(a["plaq"] - b["plaq"]) < 1e-7, (a, b)
+
+
+def test_flow_checkpoint_resume(tmp_path):
+    """A flow stopped at t = 0.1 and continued from its checkpoint to t = 0.2
+    gives bitwise the links and records of the uninterrupted flow."""
+    U = generate.random_field((4, 4, 6, 4), 0.4, 8)
+    ck = str(tmp_path / "flow.pt")
+    full, r_full = flow.wilson_flow(U, eps=0.02, tmax=0.2, measure_every=0.05)
+    flow.wilson_flow(U, eps=0.02, tmax=0.1, measure_every=0.05, checkpoint=ck)  # "interrupted" at t = 0.1
+    resumed, r_res = flow.wilson_flow(U, eps=0.02, tmax=0.2, measure_every=0.05, checkpoint=ck)
+    assert np.array_equal(resumed.to_numpy(), full.to_numpy())
+    assert r_res == r_full
+    with pytest.raises(ValueError):
+        flow.wilson_flow(U, eps=0.01, tmax=0.2, checkpoint=ck)
