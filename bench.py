@@ -418,6 +418,16 @@ def generate_host_field(dims, eps, seed):
     return generate.random_field(dims, eps, seed)
 
 
+# DRAM bytes (read + write) per site of one device step, from the ncu capture of this bench
+# (profiles/dram_traffic_b2_step_32x64.md: 16 time slabs at 32^3x64, reconstruct-12).
+TRAFFIC_PER_SITE = {("r12", (64, 32, 32, 32)): 4313.0}
+
+
+def step_traffic(prec, dims):
+    b = TRAFFIC_PER_SITE.get((prec, tuple(dims)))
+    return None if b is None else b * dims[0] * dims[1] * dims[2] * dims[3]
+
+
 def main():
     args = parse()
     dims = tuple(int(v) for v in args.dims.split(","))
@@ -610,7 +620,8 @@ def main():
         "e2e": {"value": e2e_val, "unit": "sites/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d + 8,
                 "s_per_step": e2e_s, "api": "flue_magnetic_force_c (host complex64 in, host gradient out)"},
         "roofline": {"bound": "hbm", "kernel": "whole fwd+bwd step (metric's %HBM)", "achieved": achieved_gbs,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak, "traffic": None,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                     "traffic": step_traffic(args.prec, dims),
                      "peak_source": peak_src, "alg_bytes_per_site": ALG_BYTES[args.prec]},
         "compute_roofline": {"bound": "fp32_cuda_core", "kernel": "k_linecot (line cotangents)",
                              "achieved": lc_tflops, "peak": fp32_peak_tflops, "unit": "TFLOP/s",
