@@ -152,6 +152,21 @@ def test_translation_invariance(rnd):
     assert _rel(oracle.magnetic(Ur), oracle.magnetic(rnd)) < 1e-12
 
 
+def test_haar_field_statistics():
+    """Haar-random SU(3) links: every plaquette and Polyakov loop is itself
+    Haar distributed, so E Re Tr = 0 and Var Re Tr = 1/2; the lattice averages
+    vanish within 5 standard errors, and the links are special unitary."""
+    U = generate.haar_field((6, 6, 6, 6), 11)
+    eye = np.eye(3)
+    assert np.abs(U @ np.conj(np.swapaxes(U, -1, -2)) - eye).max() < 1e-13
+    assert np.abs(np.linalg.det(U) - 1).max() < 1e-13
+    for rng in ((1, 4, 4), (2, 4, 4), (1, 1, 4)):
+        s, n = oracle.plaquette(U, *rng)
+        assert abs(s / n) < 5 * math.sqrt(0.5 / n), rng
+    s, n = oracle.polyakov(U)
+    assert abs(s / n) < 5 * math.sqrt(0.5 / n)
+
+
 def test_centre_symmetry(rnd):
     z = np.exp(2j * math.pi / 3)
     Uc = rnd.copy(order="F")
