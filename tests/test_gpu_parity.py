@@ -166,6 +166,53 @@ def test_fp32_observables(prec, tol):
     assert np.abs(a - oracle.loop5munucoord(U, 3, 2)).max() < 10 * tol
 
 
+def _host(x):
+    return x.detach().cpu().numpy() if isinstance(x, torch.Tensor) else np.asarray(x)
+
+
+@pytest.mark.parametrize("prec", ["c64", "r12"])
+def test_fp32_every_observable(U, prec):
+    """FP32 links (complex64 and reconstruct-12) against the FP64 oracle on
+    every parity lattice (odd and tiny extents, a Haar field): bounds per
+    element, absolute where sums cancel, growing with the links per loop."""
+    from flue_gb300 import forces
+
+    f = GaugeField.from_array(U, prec=prec)
+    for r in ((1, 4, 4), (2, 4, 4), (1, 1, 4)):
+        s, n, _ = G.plaquette(f, *r)
+        so, no = oracle.plaquette(U, *r)
+        assert n == no and abs(s - so) < 1e-5 * n, r
+    if U.shape[0] >= 3:
+        s, n, _ = G.polyakov(f)
+        so, no = oracle.polyakov(U)
+        assert n == no and abs(s - so) < 3e-6 * U.shape[0] * n
+    for args in ((2, 3, 2, 1), (1, 4, 1, 2), (4, 2, 3, 3)):
+        assert abs(G.wmunu(f, *args) - oracle.wmunu(U, *args)) < 2e-5, args
+    assert abs(G.wmunutau(f, 1, 2, 4, 2, 1) - oracle.wmunutau(U, 1, 2, 4, 2, 1)) < 2e-5
+    tab = _host(G.wmunu_table(f, 3, 4, 3, 2))
+    for r in range(3):
+        for t in range(2):
+            assert abs(tab[r, t] - oracle.wmunu(U, 3, 4, r + 1, t + 1)) < 2e-5, (r, t)
+    path = [2, 3, -2, 4, -3, -4, 1, -1]
+    gp = _host(G.genericpath(f, [1, 1, 1, 1], path))
+    assert np.abs(gp - oracle.genericpath(U, [1, 1, 1, 1], path)).max() < 1e-5
+    assert np.abs(_host(G.genericpath_all(f, path)) - oracle.genericpath_all(U, path)).max() < 1e-5
+    for mu, nu in ((1, 2), (3, 4)):
+        c = _host(G.cloverloopmunucoord(f, mu, nu))
+        assert np.abs(c - oracle.cloverloopmunucoord(U, mu, nu)).max() < 1e-5, (mu, nu)
+        q = _host(G.loop5munucoord(f, mu, nu))
+        assert np.abs(q - oracle.loop5munucoord(U, mu, nu)).max() < 5e-5, (mu, nu)
+    b = G.magnetic(f)
+    bo = oracle.magnetic(U)
+    assert abs(b - bo) < 1e-4 * max(1.0, abs(bo))
+    b, g = forces.magnetic_force(f)
+    g = _host(g).astype(np.complex128)
+    go = oracle.loop5_energy_force(U, oracle.B2_PLANES)
+    assert abs(b - bo) < 1e-4 * max(1.0, abs(bo))
+    assert np.linalg.norm(g - go) < 5e-5 * np.linalg.norm(go)
+    assert np.abs(g - go).max() < 1e-4 * np.abs(go).max()
+
+
 # ---------------------------------------------------------------------------
 # the host-buffer tier (reference signatures) through ctypes
 # ---------------------------------------------------------------------------
