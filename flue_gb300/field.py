@@ -15,6 +15,7 @@ global sums.
 """
 from __future__ import annotations
 
+import collections
 import ctypes
 from typing import Tuple
 
@@ -43,18 +44,25 @@ def _ptr(t: torch.Tensor):
 class Workspace:
     """Scratch buffers reused across calls (allocated by torch), one per
     (device, stream): calls queued on the same stream run in order and can
-    share one, calls on different streams may run at once and must not."""
+    share one, calls on different streams may run at once and must not.
+    At most MAX_ENTRIES buffers are kept, the least recently used dropped
+    first; torch hands a dropped buffer's memory only to later allocations on
+    the same stream, so work still queued with it is unaffected."""
 
-    _bufs = {}
+    MAX_ENTRIES = 8
+    _bufs = collections.OrderedDict()
 
     @classmethod
     def get(cls, nbytes: int, device) -> torch.Tensor:
         dev = torch.device(device)
-        key = (dev.index or 0, torch.cuda.current_stream(dev).cuda_stream)
-        buf = cls._bufs.get(key)
+        idx = dev.index if dev.index is not None else torch.cuda.current_device()
+        key = (idx, torch.cuda.current_stream(idx).cuda_stream)
+        buf = cls._bufs.pop(key, None)
         if buf is None or buf.numel() < nbytes:
-            buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
-            cls._bufs[key] = buf
+            buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=torch.device("cuda", idx))
+        cls._bufs[key] = buf
+        while len(cls._bufs) > cls.MAX_ENTRIES:
+            cls._bufs.popitem(last=False)
         return buf
 
     @classmethod
@@ -197,6 +205,11 @@ def as_field(data, prec: str | None = None) -> GaugeField:
 
 
 def workspace(op: int, field: GaugeField) -> torch.Tensor:
+    # the library launches on the calling thread's current device and stream
+    cur = torch.cuda.current_device()
+    if field.device.index != cur:
+        raise ValueError(f"field lives on {field.device} but the current device is cuda:{cur}; "
+                         f"call under torch.cuda.device({field.device.index})")
     nt, nx, ny, nz = field.dims
     n = _lib.load().flue_workspace_bytes(op, nt, nx, ny, nz, PRECS[field.prec])
     return Workspace.get(n, field.device)

@@ -64,3 +64,20 @@ def test_nan_links_propagate_and_leave_the_library_usable(prec):
     assert np.isnan(G.plaquette(GaugeField.from_array(bad, prec=prec), 1, 4, 4)[0])
     again = forces.magnetic_force(GaugeField.from_array(U, prec=prec))[0]
     assert again == clean
+
+
+def test_workspace_cache_is_bounded_across_streams():
+    """Calls on many streams get their own scratch; the cache keeps at most
+    MAX_ENTRIES buffers and every call still gives the same B^2."""
+    import torch
+
+    from flue_gb300.field import GaugeField, Workspace
+
+    f = GaugeField.from_array(generate.random_field((4, 4, 4, 4), 0.4, 51), prec="r12")
+    ref = G.magnetic(f)
+    streams = [torch.cuda.Stream() for _ in range(3 * Workspace.MAX_ENTRIES)]
+    for s in streams:
+        with torch.cuda.stream(s):
+            assert G.magnetic(f) == ref
+    torch.cuda.synchronize()
+    assert len(Workspace._bufs) <= Workspace.MAX_ENTRIES
