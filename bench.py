@@ -516,6 +516,24 @@ def main():
     L.flue_stage_timing(0)
     torch.cuda.synchronize()
 
+    # --- forward only: B^2 without the gradient, the reference's magnetic()
+    # (src/wloops.F90:479-544) -- what the reference arm times ---
+    def fwd32():
+        rc = L.flue_magnetic(ctypes.byref(d32), _ptr(b32), _ptr(w32), w32.numel(), sh)
+        if rc:
+            raise RuntimeError(L.flue_last_error_detail().decode())
+
+    for _ in range(2):
+        fwd32()
+    torch.cuda.synchronize()
+    nfwd = max(3, min(args.steps, 20))
+    e0.record()
+    for _ in range(nfwd):
+        fwd32()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_fwd = max_over_ranks(wsz, e0.elapsed_time(e1) / nfwd)
+
     # --- FP64 (complex128) GPU kernels: the denominator of the FP32 speed-up ---
     d64, w64, b64, g64 = prep(f64)
 
@@ -616,6 +634,8 @@ def main():
         "fp32_over_fp64": value / value64,
         "fp32_error_vs_fp64": {"b2_rel": rel_b, "grad_rel_l2": rel_g, "grad_rel_max": gmax, "b2_fp64": B64},
         "stages_ms": stage_ms,
+        "forward_only": {"value": wsz * V / (ms_fwd * 1e-3), "unit": "sites/s", "ms_per_step": ms_fwd,
+                         "steps": nfwd, "what": "flue_magnetic: B^2 without the gradient (the reference's magnetic)"},
         "gpu_launches": int(n_launches),
         "e2e": {"value": e2e_val, "unit": "sites/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d + 8,
                 "s_per_step": e2e_s, "api": "flue_magnetic_force_c (host complex64 in, host gradient out)"},
