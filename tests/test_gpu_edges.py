@@ -81,3 +81,33 @@ def test_workspace_cache_is_bounded_across_streams():
             assert G.magnetic(f) == ref
     torch.cuda.synchronize()
     assert len(Workspace._bufs) <= Workspace.MAX_ENTRIES
+
+
+@pytest.mark.parametrize("dims", [(1, 4, 4, 4), (2, 3, 4, 5), (3, 2, 2, 2)])
+@pytest.mark.parametrize("slabs", ["1", "99"])
+def test_host_buffer_force_small_extents(dims, slabs, monkeypatch):
+    """flue_magnetic_force_c on lattices with extents 1-3, as one pass and as
+    one-slice slabs (FLUE_SLABS above NT): the device path's B^2 and gradient."""
+    import ctypes
+
+    import torch
+
+    from flue_gb300 import _lib
+    from flue_gb300.field import GaugeField
+
+    U = generate.random_field(dims, 0.5, 52)
+    b0, g0 = forces.magnetic_force(GaugeField.from_array(U, prec="c64"))
+    g0 = g0.detach().cpu().numpy()
+    host = torch.as_tensor(np.asfortranarray(U.astype(np.complex64))).permute(6, 5, 4, 3, 2, 1, 0)
+    host = host.contiguous().pin_memory()
+    grad = torch.full_like(host, float("nan")).pin_memory()
+    monkeypatch.setenv("FLUE_SLABS", slabs)
+    L = _lib.load()
+    b = ctypes.c_double()
+    rc = L.flue_magnetic_force_c(ctypes.c_void_p(host.data_ptr()), _lib.C64, *dims, _lib.C64, _lib.FORCE_LIE,
+                                 ctypes.byref(b), ctypes.c_void_p(grad.data_ptr()))
+    assert rc == 0, L.flue_last_error_detail()
+    g = grad.permute(6, 5, 4, 3, 2, 1, 0).numpy()
+    assert np.isfinite(g).all()
+    assert abs(b.value - b0) < 1e-12 * max(1.0, abs(b0))
+    assert np.abs(g - g0).max() < 1e-6 * np.abs(g0).max()
