@@ -433,11 +433,14 @@ struct MatPlanes {
     }
 };
 
-// Pipeline intermediates, one matrix per (plane k, site s) stored contiguously
-// so that a thread fetches it with 128-bit loads from a single address:
-// FP32 18 reals padded to 5 float4 (80 B), FP64 18 reals as 9 double2
-// (144 B).  A warp reading 32 consecutive sites still touches one contiguous
-// 2.5 / 4.5 KB range, so every sector it fetches is fully used.
+// Pipeline intermediates, one matrix per (plane k, site s).
+// FP32: 18 reals padded to 5 float4 units, stored in tiles of 32 sites (a
+// warp's width) with the units unit-major inside a tile: unit u of site s of
+// plane k at float4 index ((k * T + s / 32) * 5 + u) * 32 + s % 32, T = the
+// number of tiles.  A warp reading one unit of 32 consecutive sites then
+// reads 512 contiguous bytes (4 cache lines) -- against 20 lines for 32
+// matrices at an 80-byte stride -- with the same 5 load instructions per
+// matrix.  FP64: 18 reals as 9 double2 per (plane, site), contiguous (144 B).
 template <typename T>
 struct MatAoS;
 template <>
@@ -448,32 +451,36 @@ struct MatAoS<float> {
     __device__ __forceinline__ bool ok(int64_t s, int k) const {
         return FLUE_INB(s >= 0 && s < V && k >= 0 && (nk == 0 || k < nk));
     }
+    __device__ __forceinline__ const float4* unit0(int64_t s, int k) const {
+        return p + (((int64_t)k * ((V + 31) >> 5) + (s >> 5)) * 5) * 32 + (s & 31);
+    }
     __device__ __forceinline__ M3<float> load(int64_t s, int k) const {
         if (!ok(s, k)) return m_zero<float>();
-        const float4* q = p + ((int64_t)k * V + s) * 5;
+        const float4* q = unit0(s, k);
         M3<float> m;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float4 v = q[j];
+            const float4 v = q[32 * j];
             m.r[2 * j] = v.x;
             m.i[2 * j] = v.y;
             m.r[2 * j + 1] = v.z;
             m.i[2 * j + 1] = v.w;
         }
-        const float4 v = q[4];
+        const float4 v = q[128];
         m.r[8] = v.x;
         m.i[8] = v.y;
         return m;
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<float>& m) const {
         if (!ok(s, k)) return;
-        float4* q = p + ((int64_t)k * V + s) * 5;
+        float4* q = const_cast<float4*>(unit0(s, k));
 #pragma unroll
-        for (int j = 0; j < 4; ++j) q[j] = make_float4(m.r[2 * j], m.i[2 * j], m.r[2 * j + 1], m.i[2 * j + 1]);
-        q[4] = make_float4(m.r[8], m.i[8], 0.f, 0.f);
+        for (int j = 0; j < 4; ++j) q[32 * j] = make_float4(m.r[2 * j], m.i[2 * j], m.r[2 * j + 1], m.i[2 * j + 1]);
+        q[128] = make_float4(m.r[8], m.i[8], 0.f, 0.f);
     }
     static constexpr size_t bytes_per_matrix = 80;
-    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 5; }
+    // bytes of nk planes over V sites (V rounded up to whole tiles)
+    static size_t bytes(int64_t V, int64_t nk) { return (size_t)nk * (size_t)((V + 31) & ~(int64_t)31) * 80; }
 };
 template <>
 struct MatAoS<double> {
@@ -502,7 +509,7 @@ struct MatAoS<double> {
         for (int e = 0; e < 9; ++e) q[e] = make_double2(m.r[e], m.i[e]);
     }
     static constexpr size_t bytes_per_matrix = 144;
-    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 9; }
+    static size_t bytes(int64_t V, int64_t nk) { return (size_t)nk * (size_t)V * 144; }
 };
 
 // Anti-Hermitian matrix per (plane k, site s), contiguous: Im F00, Im F11,
@@ -599,39 +606,43 @@ template <typename T>
 struct AHAoS;
 template <>
 struct AHAoS<float> {
+    // 9 reals padded to 3 float4 units, tiled by 32 sites as MatAoS<float>:
+    // unit u of site s of plane k at ((k * T + s / 32) * 3 + u) * 32 + s % 32
     float4* __restrict__ p;
     int64_t V;
     int nk = 0;  // planes, checked when > 0 (bounds-checked build)
     __device__ __forceinline__ bool ok(int64_t s, int k) const {
         return FLUE_INB(s >= 0 && s < V && k >= 0 && (nk == 0 || k < nk));
     }
+    __device__ __forceinline__ const float4* unit0(int64_t s, int k) const {
+        return p + (((int64_t)k * ((V + 31) >> 5) + (s >> 5)) * 3) * 32 + (s & 31);
+    }
     __device__ __forceinline__ void load_packed(int64_t s, int k, float v[9]) const {
         if (!ok(s, k)) {
             for (int e = 0; e < 9; ++e) v[e] = 0;
             return;
         }
-        const float4* q = p + ((int64_t)k * V + s) * 3;
-        const float4 a = q[0], b = q[1], c = q[2];
+        const float4* q = unit0(s, k);
+        const float4 a = q[0], b = q[32], c = q[64];
         v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w;
         v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
         v[8] = c.x;
     }
     __device__ __forceinline__ M3<float> load(int64_t s, int k) const {
         if (!ok(s, k)) return m_zero<float>();
-        const float4* q = p + ((int64_t)k * V + s) * 3;
-        const float4 a = q[0], b = q[1], c = q[2];
-        const float v[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+        float v[9];
+        load_packed(s, k, v);
         return ah_expand<float>(v);
     }
     __device__ __forceinline__ void store(int64_t s, int k, const M3<float>& m) const {
         if (!ok(s, k)) return;
-        float4* q = p + ((int64_t)k * V + s) * 3;
+        float4* q = const_cast<float4*>(unit0(s, k));
         q[0] = make_float4(m.i[0], m.i[4], m.i[8], m.r[1]);
-        q[1] = make_float4(m.i[1], m.r[2], m.i[2], m.r[5]);
-        q[2] = make_float4(m.i[5], 0.f, 0.f, 0.f);
+        q[32] = make_float4(m.i[1], m.r[2], m.i[2], m.r[5]);
+        q[64] = make_float4(m.i[5], 0.f, 0.f, 0.f);
     }
     static constexpr size_t bytes_per_matrix = 48;
-    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 3; }
+    static size_t bytes(int64_t V, int64_t nk) { return (size_t)nk * (size_t)((V + 31) & ~(int64_t)31) * 48; }
 };
 template <>
 struct AHAoS<double> {
@@ -668,7 +679,7 @@ struct AHAoS<double> {
         q[4] = make_double2(m.i[5], 0.0);
     }
     static constexpr size_t bytes_per_matrix = 80;
-    __device__ __forceinline__ const void* ptr(int64_t s, int k) const { return p + ((int64_t)k * V + s) * 5; }
+    static size_t bytes(int64_t V, int64_t nk) { return (size_t)nk * (size_t)V * 80; }
 };
 
 // Anti-Hermitian matrices stored as 9 reals per site: Im F00, Im F11, Im F22,

@@ -549,14 +549,14 @@ struct EnergyWs {
 
 static EnergyWs energy_layout(const Geom& g, int prec, const PlaneArg& pa, bool with_force) {
     const bool d = prec == PREC_C128;  // FP64 intermediates
-    const size_t mat = d ? MatAoS<double>::bytes_per_matrix : MatAoS<float>::bytes_per_matrix;
-    const size_t ah = d ? AHAoS<double>::bytes_per_matrix : AHAoS<float>::bytes_per_matrix;
+    auto mat = [&](int64_t nk) { return d ? MatAoS<double>::bytes(g.V, nk) : MatAoS<float>::bytes(g.V, nk); };
+    auto ah = [&](int64_t nk) { return d ? AHAoS<double>::bytes(g.V, nk) : AHAoS<float>::bytes(g.V, nk); };
     EnergyWs w;
     const int nbx = (int)((g.V + FWD_BS - 1) / FWD_BS);
     w.lines = 0;
-    w.kbuf = align256(w.lines + (size_t)(FLUE_LINES_DAG ? 6 : 3) * pa.nd * g.V * mat);
-    w.lam = align256(w.kbuf + (with_force ? (size_t)pa.np * g.V * ah : 0));
-    w.part = align256(w.lam + (with_force ? (size_t)3 * pa.nd * g.V * mat : 0));
+    w.kbuf = align256(w.lines + mat((FLUE_LINES_DAG ? 6 : 3) * pa.nd));
+    w.lam = align256(w.kbuf + (with_force ? ah(pa.np) : 0));
+    w.part = align256(w.lam + (with_force ? mat(3 * pa.nd) : 0));
     w.total = align256(w.part + (size_t)pa.np * nbx * sizeof(double));
     return w;
 }

@@ -481,18 +481,22 @@ __global__ void __launch_bounds__(WT_BS) k_wt_loops(Geom g, int mu, int nu, int 
     if (threadIdx.x == 0) part[(int64_t)rt * nsb + sb] = r;
 }
 
+// the stored mu- and nu-lines of every length, rounded to 256 bytes
+static size_t wt_lines_bytes(const Geom& g, int prec, int rmax, int tmax) {
+    const size_t b = prec == PREC_C128 ? MatAoS<double>::bytes(g.V, rmax + tmax) : MatAoS<float>::bytes(g.V, rmax + tmax);
+    return (b + 255) & ~(size_t)255;
+}
+
 size_t wmunu_table_ws_bytes(const Geom& g, int prec, int rmax, int tmax) {
-    const size_t bpm = prec == PREC_C128 ? MatAoS<double>::bytes_per_matrix : MatAoS<float>::bytes_per_matrix;
     const size_t nsb = (size_t)((g.V + WT_BS - 1) / WT_BS);
-    const size_t lines = (((size_t)(rmax + tmax) * g.V * bpm) + 255) & ~(size_t)255;
+    const size_t lines = wt_lines_bytes(g, prec, rmax, tmax);
     return lines + (((size_t)rmax * tmax * nsb * sizeof(double) + 255) & ~(size_t)255);
 }
 
 cudaError_t launch_wmunu_table(const FieldRef& U, int mu, int nu, int rmax, int tmax, double* out, void* ws,
                                cudaStream_t st) {
     const Geom& g = U.g;
-    const size_t bpm = U.prec == PREC_C128 ? MatAoS<double>::bytes_per_matrix : MatAoS<float>::bytes_per_matrix;
-    const size_t lines_b = (((size_t)(rmax + tmax) * g.V * bpm) + 255) & ~(size_t)255;
+    const size_t lines_b = wt_lines_bytes(g, U.prec, rmax, tmax);
     double* part = (double*)((char*)ws + lines_b);
     const unsigned nsb = (unsigned)((g.V + WT_BS - 1) / WT_BS);
     const unsigned nrt = (unsigned)(rmax * tmax);
