@@ -420,7 +420,7 @@ def generate_host_field(dims, eps, seed):
 
 # DRAM bytes (read + write) per site of one device step, from the ncu capture of this bench
 # (profiles/dram_traffic_b2_step_32x64.md: 16 time slabs at 32^3x64, reconstruct-12).
-TRAFFIC_PER_SITE = {("r12", (64, 32, 32, 32)): 4313.0}
+TRAFFIC_PER_SITE = {("r12", (64, 32, 32, 32)): 4325.0}
 
 
 def step_traffic(prec, dims):
