@@ -159,6 +159,9 @@ __device__ __forceinline__ int64_t patch_site(const Geom& g, const PatchArg& pt,
            (int64_t)(bo * pt.po + io) * sto;
 }
 
+#ifndef FLUE_PATCH_MIN_TW
+#define FLUE_PATCH_MIN_TW 8
+#endif
 static PatchArg make_patch(const Geom& g, const PlaneArg& pa, int bs) {
     PatchArg pt{0, 1, 1, 1};
     int tw = 1;
@@ -171,9 +174,10 @@ static PatchArg make_patch(const Geom& g, const PlaneArg& pa, int bs) {
         const int mu = pa.mu[q], nu = pa.nu[q], od = 6 - mu - nu;
         if (mu <= 0 || nu <= 0 || g.n[mu] % pm || g.n[nu] % pm || g.n[od] % po) return pt;
     }
-    // warps must keep runs of >= 8 consecutive sites (coalescing); with 4
-    // time slices the patch traversal measured slower than the linear one
-    if (tw * pm * pm * po != bs || tw < 8) return pt;
+    // warps keep runs of >= FLUE_PATCH_MIN_TW consecutive sites (measured at
+    // 32^3x64 in 4-slice slabs, tiled intermediates: minimum 4 -> 10.74 ms a
+    // step, 8 -> 10.50 ms)
+    if (tw * pm * pm * po != bs || tw < FLUE_PATCH_MIN_TW) return pt;
     pt.tw = tw;
     pt.pm = pt.pn = pm;
     pt.po = po;
