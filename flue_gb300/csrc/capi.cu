@@ -468,7 +468,7 @@ struct DevCache {
     // high-priority streams that stream slabs in (pack) and gradients out
     // beside the compute on `st` (and up to kPipeComp - 1 more compute
     // streams), a ring of kPipeComp + 1 buffer slots (packed slab + workspace)
-    static constexpr int kPipeComp = 3, kPipeSlots = kPipeComp + 1;
+    static constexpr int kPipeComp = 4, kPipeSlots = kPipeComp + 1;
     bool pipe_init = false;
     cudaStream_t s_in = nullptr, s_out = nullptr, s_cp[kPipeComp - 1] = {};
     cudaEvent_t ev_go = nullptr, ev_in[kPipeSlots] = {}, ev_cp[kPipeSlots] = {}, ev_out[kPipeSlots] = {},
@@ -706,7 +706,8 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
     const size_t wbytes = energy_ws_bytes(g0, prec, ps, d_grad != nullptr);
     // compute streams (FLUE_PIPE_STREAMS, default 3): slab k computes on
     // stream k % ncomp, so the compute of neighbouring slabs overlaps too
-    // (measured at 64x32^3, 8 slabs: 12.5 ms on 1 stream, 11.9 on 2, 11.8 on 3)
+    // (measured at 64x32^3, 8 slabs: 12.5 ms on 1 stream, 11.9 on 2, 11.8 on 3;
+    // 16 slabs: 11.7 on 2, 11.4 on 3 and on 4)
     int ncomp = env_int("FLUE_PIPE_STREAMS", 3);
     ncomp = ncomp < 1 ? 1 : (ncomp > DevCache::kPipeComp ? DevCache::kPipeComp : ncomp);
     const int nslot = ncomp + 1;
