@@ -94,10 +94,13 @@ __device__ __forceinline__ int wrapd(int c, int k, int n) {
 }
 
 // FLUE_LINES_DAG = 1 keeps daggered copies of the lines so that the line
-// cotangents need no select instructions for S3, S4 (twice the line storage;
-// measured slower on GB300, off by default)
+// cotangents need no select instructions for S3, S4 (twice the line storage).
+// Measured on GB300 at 32^3x64 with the tiled intermediates: k_lines 0.27 ->
+// 0.50 ms, k_linecot 7.22 -> 6.84 ms, the 16-slab step 10.46 -> 10.21 ms (with
+// the earlier 80-byte-stride layout the extra line writes cost more than the
+// selects saved).
 #ifndef FLUE_LINES_DAG
-#define FLUE_LINES_DAG 0
+#define FLUE_LINES_DAG 1
 #endif
 
 // Traversal order of the site blocks of the stencil kernels.  The lattice is
@@ -248,7 +251,7 @@ __device__ __forceinline__ void corner_off(int k, int a, int b, int& di, int& dj
 //    never step in time then).
 // ---------------------------------------------------------------------------
 template <class L, typename T>
-__global__ void k_lines(L U, Geom g, Geom gs, int t0, PlaneArg pa, MatAoS<T> lines) {
+__global__ void k_lines(L U, Geom g, Geom gs, int t0, PlaneArg pa, MatAoS<T> lines, int dag_copies) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     const int slot = blockIdx.y;
@@ -271,10 +274,12 @@ __global__ void k_lines(L U, Geom g, Geom gs, int t0, PlaneArg pa, MatAoS<T> lin
     lines.store(s, 3 * slot + 2, l3);
 #if FLUE_LINES_DAG
     // daggered copies after the 3 * nd plain lines (the line cotangents read
-    // S3, S4 = L^+ without select instructions)
-    lines.store(s, 3 * (pa.nd + slot), dag(u0));
-    lines.store(s, 3 * (pa.nd + slot) + 1, dag(l2));
-    lines.store(s, 3 * (pa.nd + slot) + 2, dag(l3));
+    // S3, S4 = L^+ without select instructions; only they use the copies)
+    if (dag_copies) {
+        lines.store(s, 3 * (pa.nd + slot), dag(u0));
+        lines.store(s, 3 * (pa.nd + slot) + 1, dag(l2));
+        lines.store(s, 3 * (pa.nd + slot) + 2, dag(l3));
+    }
 #endif
 }
 
@@ -622,7 +627,8 @@ static cudaError_t energy_fwd_part(const L& U, const Geom& g, const Geom& gs, in
     double* part = out_E ? (double*)(ws + w.part) : nullptr;
     const unsigned nbx = (unsigned)((g.V + FWD_BS - 1) / FWD_BS);
     stage_mark(0, st);
-    note_launch(), k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, gs, t0, pa, lines);
+    note_launch(), k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, gs, t0, pa, lines,
+                                                                                         with_force ? 1 : 0);
     stage_mark(1, st);
     const PatchArg pt = FLUE_FWD_PATCH ? make_patch(g, pa, FWD_BS) : PatchArg{};
     note_launch(), k_fwd<T><<<nbx * pa.np, FWD_BS, 0, st>>>(g, pa, kind, pt, lines, kb, fout, part);
