@@ -563,7 +563,8 @@ static EnergyWs energy_layout(const Geom& g, int prec, const PlaneArg& pa, bool 
     EnergyWs w;
     const int nbx = (int)((g.V + FWD_BS - 1) / FWD_BS);
     w.lines = 0;
-    w.kbuf = align256(w.lines + mat((FLUE_LINES_DAG ? 6 : 3) * pa.nd));
+    // daggered line copies only when the line cotangents run
+    w.kbuf = align256(w.lines + mat((FLUE_LINES_DAG && with_force ? 6 : 3) * pa.nd));
     w.lam = align256(w.kbuf + (with_force ? ah(pa.np) : 0));
     w.part = align256(w.lam + (with_force ? mat(3 * pa.nd) : 0));
     w.total = align256(w.part + (size_t)pa.np * nbx * sizeof(double));
