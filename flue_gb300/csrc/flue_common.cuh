@@ -401,38 +401,6 @@ struct R12Links {
     }
 };
 
-// Generic matrix planes: matrix k of site s, element e (row-major 3a+b) at
-// base[(k*9 + e)*V + s].  Used for intermediates (lines, cotangents).
-template <typename T>
-struct MatPlanes {
-    using C2 = typename V2<T>::type;
-    C2* __restrict__ p;
-    int64_t V;
-    __device__ __forceinline__ M3<T> load(int64_t s, int k) const {
-        M3<T> m;
-        if (!FLUE_INB(s >= 0 && s < V && k >= 0)) return m_zero<T>();
-        const C2* q = p + (int64_t)k * 9 * V + s;
-#pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            const C2 v = q[e * V];
-            m.r[e] = v.x;
-            m.i[e] = v.y;
-        }
-        return m;
-    }
-    __device__ __forceinline__ void store(int64_t s, int k, const M3<T>& m) const {
-        if (!FLUE_INB(s >= 0 && s < V && k >= 0)) return;
-        C2* q = p + (int64_t)k * 9 * V + s;
-#pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            C2 v;
-            v.x = m.r[e];
-            v.y = m.i[e];
-            q[e * V] = v;
-        }
-    }
-};
-
 // Pipeline intermediates, one matrix per (plane k, site s).
 // FP32: 18 reals padded to 5 float4 units, stored in tiles of 32 sites (a
 // warp's width) with the units unit-major inside a tile: unit u of site s of
