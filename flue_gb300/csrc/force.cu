@@ -197,20 +197,6 @@ struct Ctx {
     int cm, cn, nm, nn;  // coordinates and extents along mu, nu
     int64_t stm, stn;    // site strides along mu, nu
     int kmu, knu;        // first line plane of the mu / nu slot (3 * slot)
-    __device__ __forceinline__ int64_t at(int i, int j) const {
-        return s + (int64_t)wrapd(cm, i, nm) * stm + (int64_t)wrapd(cn, j, nn) * stn;
-    }
-    // side k (1..4) of the rectangle anchored at (i0,j0) with shape (a,b):
-    // S1 = L^a_mu(i0,j0), S2 = L^b_nu(i0+a,j0), S3 = L^a_mu(i0,j0+b)^+,
-    // S4 = L^b_nu(i0,j0)^+.  Selected arithmetically (one load site in the
-    // code for any k) to keep the kernels' instruction footprint small.
-    __device__ __forceinline__ M3<T> side(int k, int i0, int j0, int a, int b) const {
-        const bool isnu = (k & 1) == 0;
-        const int plane = isnu ? knu + b - 1 : kmu + a - 1;
-        const int i = i0 + (k == 2 ? a : 0), j = j0 + (k == 3 ? b : 0);
-        const M3<T> m = lines.load(at(i, j), plane);
-        return k >= 3 ? dag(m) : m;
-    }
 };
 
 template <typename T>
@@ -238,10 +224,6 @@ __device__ __forceinline__ Ctx<T> make_ctx(const MatAoS<T>& lines, const Geom& g
     return cx;
 }
 
-__device__ __forceinline__ void corner_off(int k, int a, int b, int& di, int& dj) {
-    di = (k == 2 || k == 3) ? a : 0;
-    dj = (k == 3 || k == 4) ? b : 0;
-}
 
 // ---------------------------------------------------------------------------
 // 1. lines: L^1_d(y) = U_d(y) (expanded to 18 reals), L^2_d(y) = U_d(y) U_d(y+d),
@@ -387,14 +369,6 @@ __global__ void __launch_bounds__(FWD_BS, MinBlocks<T>::fwd)
 // ---------------------------------------------------------------------------
 constexpr int COT_BS = FLUE_COT_BS;
 
-// packed anti-Hermitian cotangent K (9 reals) at corner k of the rectangle
-template <typename T>
-__device__ __forceinline__ void corner_k(const Ctx<T>& cx, const AHAoS<T>& kin, int p, int k, int i0, int j0, int a,
-                                         int b, T v[9]) {
-    int di, dj;
-    corner_off(k, a, b, di, dj);
-    kin.load_packed(cx.at(i0 + di, j0 + dj), p, v);
-}
 
 // Sum of the four corner insertions in the word that follows side q of the
 // rectangle (i0,j0,a,b):  Ka A B C + A Kb B C + A B Kc C + A B C Kd with
