@@ -20,14 +20,19 @@ namespace {
 
 thread_local char g_detail[256] = "";
 
+int fail(int code, const char* msg) {
+    snprintf(g_detail, sizeof(g_detail), "%s", msg);
+    return code;
+}
+
+}  // namespace
+
+namespace flue {
+
 int cuda_status(cudaError_t e) {
     if (e == cudaSuccess) return FLUE_OK;
     snprintf(g_detail, sizeof(g_detail), "%s: %s", cudaGetErrorName(e), cudaGetErrorString(e));
     return FLUE_ERR_CUDA;
-}
-int fail(int code, const char* msg) {
-    snprintf(g_detail, sizeof(g_detail), "%s", msg);
-    return code;
 }
 
 bool dims_ok(int nt, int nx, int ny, int nz) {
@@ -49,6 +54,10 @@ int check_field(const flue_field* U, FieldRef* out) {
     out->prec = U->prec;
     return FLUE_OK;
 }
+
+}  // namespace flue
+
+namespace {
 
 inline size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 

@@ -8,6 +8,8 @@
 
 #include "flue_common.cuh"
 
+struct flue_field;
+
 namespace flue {
 
 struct FieldRef {
@@ -109,6 +111,17 @@ unsigned oob_propagator();
 
 // text returned by flue_last_error_detail() on the calling thread
 void set_error_detail(const char* msg);
+
+// Argument checks shared by every device entry point (capi.cu): a NULL
+// descriptor or links pointer, an unknown precision, bad extents and a links
+// pointer off its element alignment (8 bytes for C64, 16 for C128 / R12) are
+// refused with a status code and a detail text before anything is launched.
+bool dims_ok(int nt, int nx, int ny, int nz);
+bool prec_ok(int p);
+int check_field(const ::flue_field* U, FieldRef* out);
+// FLUE_OK for cudaSuccess, else FLUE_ERR_CUDA with the error's name and text
+// as the detail
+int cuda_status(cudaError_t e);
 
 // process-wide count of kernel launches (flue_kernel_launches); every launch
 // site calls it as `note_launch(), kernel<<<...>>>(...)`

@@ -16,7 +16,9 @@
 // last call; the kernel writes every slot it later reads, so nothing has to
 // be cleared between calls.  Two calls whose work overlaps on the GPU (for
 // example on two streams at once) race on the array and can both return
-// wrong sums: serialise them.
+// wrong sums: serialise them.  The array's address is looked up on the first
+// call on each device and kept, so this entry point must not be used across a
+// cudaDeviceReset in the same process.
 #include <mutex>
 
 #include "../../include/flue_gb300.h"
@@ -34,7 +36,9 @@ double* g_noalloc_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device, looked up once
 // per device.  Host code sees only a host-side stand-in for the symbol, so
-// the address must come from cudaGetSymbolAddress.
+// the address must come from cudaGetSymbolAddress.  The cached address is
+// not refreshed: after cudaDeviceReset the module may load elsewhere, so the
+// entry point must not be used across a device reset in one process.
 cudaError_t scratch_on_current_device(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -55,27 +59,19 @@ cudaError_t scratch_on_current_device(double** out) {
 
 extern "C" int flue_plaquette_noalloc(const flue_field* U, int muStart, int muEnd, int nuEnd, double* d_sum,
                                       void* stream) {
-    if (!U || !U->links || !d_sum) {
-        flue::set_error_detail("flue_plaquette_noalloc: NULL field, links or output pointer");
+    // the same validator as flue_plaquette: NULL pointers, precision,
+    // extents and the links pointer's alignment are refused before launch
+    flue::FieldRef F;
+    int rc = flue::check_field(U, &F);
+    if (rc) return rc;
+    if (!d_sum) {
+        flue::set_error_detail("flue_plaquette_noalloc: NULL output pointer");
         return FLUE_ERR_ARG;
-    }
-    if (U->prec != FLUE_C128 && U->prec != FLUE_C64 && U->prec != FLUE_R12) {
-        flue::set_error_detail("flue_plaquette_noalloc: unknown field precision");
-        return FLUE_ERR_DTYPE;
-    }
-    if (U->nt < 1 || U->nx < 1 || U->ny < 1 || U->nz < 1 ||
-        (int64_t)U->nt * U->nx * U->ny * U->nz >= ((int64_t)1 << 31)) {
-        flue::set_error_detail("flue_plaquette_noalloc: bad lattice extents");
-        return FLUE_ERR_SHAPE;
     }
     if (muStart < 1 || muEnd > 4 || nuEnd > 4 || muStart > muEnd + 1 || nuEnd < 1) {
         flue::set_error_detail("flue_plaquette_noalloc: plane range out of 1..4");
         return FLUE_ERR_ARG;
     }
-    flue::FieldRef F;
-    F.links = U->links;
-    F.g = flue::make_geom(U->nt, U->nx, U->ny, U->nz);
-    F.prec = U->prec;
     // one FP64 partial per block of the plaquette kernel
     const int need = flue::plaquette_blocks(F.g);
     if (need > FLUE_NOALLOC_SCRATCH_DOUBLES) {
@@ -90,8 +86,8 @@ extern "C" int flue_plaquette_noalloc(const flue_field* U, int muStart, int muEn
         flue::set_error_detail("flue_plaquette_noalloc: cudaGetSymbolAddress of the scratch array failed");
         return FLUE_ERR_CUDA;
     }
-    cudaError_t e = flue::launch_plaquette(F, muStart - 1, muEnd - 1, nuEnd - 1, scratch, d_sum, (cudaStream_t)stream);
-    return e == cudaSuccess ? FLUE_OK : FLUE_ERR_CUDA;
+    return flue::cuda_status(
+        flue::launch_plaquette(F, muStart - 1, muEnd - 1, nuEnd - 1, scratch, d_sum, (cudaStream_t)stream));
 }
 
 namespace flue {

@@ -256,10 +256,13 @@ int flue_ensemble_destroy(flue_ensemble *e);
  * the HBM, or a framework whose allocator this library cannot reach).  Limit:
  * 1024 partial sums; the plaquette launch never uses more than 608 blocks, so
  * every lattice the ABI accepts fits, and a larger need is refused with
- * FLUE_ERR_WORKSPACE.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+ * FLUE_ERR_WORKSPACE.  The arguments are checked exactly as flue_plaquette
+ * checks them (precision, extents, links alignment).  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and
+ * keeps it; make that first call before any stream capture, and do not use
+ * this entry point across a cudaDeviceReset in the same process (the module
+ * can be reloaded at another address).  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
 int flue_plaquette_noalloc(const flue_field *U, int muStart, int muEnd, int nuEnd, double *d_sum, void *stream);
 
 /* ======================================================================== */
