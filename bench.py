@@ -347,75 +347,83 @@ def max_over_ranks(ws, v):
     return float(t.item())
 
 
-def cpu_baseline(host_c128, dims, target_s):
-    """The oracle's OpenMP magnetic() on a bounded slab of time slices."""
+def cpu_baseline(dims, eps, seed, target_s):
+    """The oracle's OpenMP magnetic() on a bounded sample: repeated passes over
+    the first time slices of the benchmark field (built on the host)."""
     import oracle
 
-    nt = dims[0]
+    U = host_slab(dims, eps, seed)
+    nts = U.shape[0]
     V3 = dims[1] * dims[2] * dims[3]
     t0 = time.perf_counter()
-    oracle.magnetic_slab(host_c128, 1, 1)
+    oracle.magnetic_slab(U, 1, nts)
     one = max(time.perf_counter() - t0, 1e-3)
-    nsl = int(max(1, min(nt, target_s / one)))
+    reps = int(max(1, round(target_s / one)))
     t0 = time.perf_counter()
-    oracle.magnetic_slab(host_c128, 1, nsl)
+    for _ in range(reps):
+        oracle.magnetic_slab(U, 1, nts)
     dt = time.perf_counter() - t0
-    return {"value": nsl * V3 / dt, "unit": "sites/s", "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"oracle magnetic() forward (B^2 only; the reference has no backward), OpenMP, time slices "
-                      f"1..{nsl} of the {dims[1]}^3x{dims[0]} field ({nsl * V3} sites, {dt:.2f} s)"}
+    return {"value": reps * nts * V3 / dt, "unit": "sites/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"oracle magnetic() forward (B^2 only; the reference has no backward), OpenMP, {reps} passes "
+                      f"over time slices 1..{nts} of the {dims[1]}^3x{dims[0]} field ({reps * nts * V3} sites, "
+                      f"{dt:.2f} s)"}
+
+
+# time slices of the field that the CPU legs generate and time: B^2 uses only
+# the spatial planes, so time slices are independent and the first nts slices
+# of the full seeded field are the field random_field((nts, NX, NY, NZ))
+CPU_SLICES = 8
+
+
+def host_slab(dims, eps, seed, nts=CPU_SLICES):
+    """The first `nts` time slices of the benchmark field, built on the host
+    with numpy only (the Gell-Mann coefficients are drawn in (t,x,y,z,mu,a)
+    order, so these slices are bitwise those of the full field's host
+    construction).  Touches neither the GPU nor this repository's library."""
+    from flue_gb300 import generate
+
+    nt, nx, ny, nz = dims
+    return generate.random_field((min(nt, nts), nx, ny, nz), eps, seed)
 
 
 def run_reference(args, dims, ws, rank):
     """--impl reference: the reference's algorithm (oracle port of wloops.F90
-    magnetic(), forward only) on the host cores; rank 0 only."""
+    magnetic(), forward only) on the host cores; rank 0 only.  The field is
+    built on the host (numpy) and the arm never loads the CUDA library."""
     if rank != 0:
         return
-    import numpy as np
-
     import oracle
-    from flue_gb300 import generate
 
     oracle.build()
-    # host field of the same configuration (generated slab-wise is not
-    # needed: the whole field is built once, then each step times a slab)
     nt, nx, ny, nz = dims
-    U = generate_host_field(dims, args.eps, args.seed)
+    U = host_slab(dims, args.eps, args.seed)
+    nts = U.shape[0]
     V3 = nx * ny * nz
     t0 = time.perf_counter()
-    oracle.magnetic_slab(U, 1, 1)
+    oracle.magnetic_slab(U, 1, nts)
     one = max(time.perf_counter() - t0, 1e-3)
     per_step_s = max(1.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
-    nsl = int(max(1, min(nt, per_step_s / one)))
+    reps = int(max(1, round(per_step_s / one)))
     for _ in range(args.warmup):
-        oracle.magnetic_slab(U, 1, nsl)
+        oracle.magnetic_slab(U, 1, nts)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.magnetic_slab(U, 1, nsl)
+        for _ in range(reps):
+            oracle.magnetic_slab(U, 1, nts)
     dt = (time.perf_counter() - t0) / args.steps
-    val = nsl * V3 / dt
+    val = reps * nts * V3 / dt
     line = {"metric": METRIC, "value": val, "unit": "sites/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": bench_config(args, dims, 1),
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": "sites/s", "cores": oracle.num_threads(), "kind": "port",
-                             "sample": f"per step: time slices 1..{nsl} of the field ({nsl * V3} sites), forward only "
+                             "sample": f"per step: {reps} x magnetic() over time slices 1..{nts} of the field "
+                                       f"({reps * nts * V3} sites, built on the host with numpy), forward only "
                                        "(the reference has no backward); Fortran reference not buildable here, "
                                        "C restatement of src/wloops.F90 timed instead"},
             "e2e": {"value": val, "unit": "sites/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
-
-
-def generate_host_field(dims, eps, seed):
-    """FP64 host copy of the benchmark field (exponentials on the GPU when one
-    is present, so that the 32^3x64 field builds in seconds)."""
-    import torch
-
-    from flue_gb300 import generate
-
-    if torch.cuda.is_available():
-        return generate.random_field(dims, eps, seed, device="cuda").to_numpy()
-    return generate.random_field(dims, eps, seed)
 
 
 # DRAM bytes (read + write) per site of one device step, from the ncu capture of this bench
@@ -552,6 +560,22 @@ def main():
     ms64 = max_over_ranks(wsz, e0.elapsed_time(e1) / args.fp64_steps)
     value64 = wsz * V / (ms64 * 1e-3)
 
+    # FP64 forward only: the reference's magnetic() at the reference's own
+    # precision -- the like-for-like GPU counterpart of the CPU figures
+    def fwd64():
+        rc = L.flue_magnetic(ctypes.byref(d64), _ptr(b64), _ptr(w64), w64.numel(), sh)
+        if rc:
+            raise RuntimeError(L.flue_last_error_detail().decode())
+
+    fwd64()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.fp64_steps):
+        fwd64()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_fwd64 = max_over_ranks(wsz, e0.elapsed_time(e1) / args.fp64_steps)
+
     # --- FP32 error against the FP64 result on the same field ---
     step32()
     torch.cuda.synchronize()
@@ -564,28 +588,37 @@ def main():
     del w64, g64
     torch.cuda.empty_cache()
 
-    # --- end to end through the host-buffer C ABI (pinned host buffers) ---
-    host_in = f32.to_tensor(torch.complex64).permute(6, 5, 4, 3, 2, 1, 0).contiguous().cpu().pin_memory()
-    host_grad = torch.empty_like(host_in).pin_memory()
-    hb = ctypes.c_double()
+    # --- end to end through the host-buffer C ABI (pinned host buffers): the
+    # field in the reference's own data type (complex128, Fortran order, as
+    # its readers produce it) in, FP32 compute in the bench precision, the
+    # complex128 gradient out; and the same with a complex64 host field ---
     prec_code = {"r12": _lib.R12, "c64": _lib.C64}[args.prec]
+    hb = ctypes.c_double()
 
-    def e2e_step():
-        rc = L.flue_magnetic_force_c(ctypes.c_void_p(host_in.data_ptr()), _lib.C64, nt, nx, ny, nz, prec_code,
-                                     _lib.FORCE_LIE, ctypes.byref(hb), ctypes.c_void_p(host_grad.data_ptr()))
-        if rc:
-            raise RuntimeError(L.flue_last_error_detail().decode())
+    def e2e_leg(host_dtype, dtype_code):
+        host_in = f64.to_tensor(host_dtype).permute(6, 5, 4, 3, 2, 1, 0).contiguous().cpu().pin_memory()
+        host_grad = torch.empty_like(host_in).pin_memory()
 
-    e2e_step()
-    barrier(wsz)
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+        def e2e_step():
+            rc = L.flue_magnetic_force_c(ctypes.c_void_p(host_in.data_ptr()), dtype_code, nt, nx, ny, nz, prec_code,
+                                         _lib.FORCE_LIE, ctypes.byref(hb), ctypes.c_void_p(host_grad.data_ptr()))
+            if rc:
+                raise RuntimeError(L.flue_last_error_detail().decode())
+
         e2e_step()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    e2e_s = max_over_ranks(wsz, e2e_s)
-    L.flue_release_host_cache()
+        barrier(wsz)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e2e_s = max_over_ranks(wsz, (time.perf_counter() - t0) / args.e2e_steps)
+        L.flue_release_host_cache()
+        nbytes = host_in.numel() * host_in.element_size()
+        del host_in, host_grad
+        return e2e_s, nbytes
+
+    e2e_s, h2d = e2e_leg(torch.complex128, _lib.C128)
     e2e_val = wsz * V / e2e_s
-    h2d = host_in.numel() * host_in.element_size()
+    e2e64_s, h2d64 = e2e_leg(torch.complex64, _lib.C64)
 
     # --- CPU baseline (rank 0, N = 1 only) ---
     cpu = None
@@ -594,8 +627,7 @@ def main():
         import oracle
 
         oracle.build()
-        host64 = f64.to_numpy()
-        cpu = cpu_baseline(host64, dims, args.cpu_seconds)
+        cpu = cpu_baseline(dims, args.eps, args.seed, args.cpu_seconds)
 
     # --- roofline ---
     peaks = {}
@@ -610,8 +642,9 @@ def main():
     achieved_gbs = ALG_BYTES[args.prec] * V / (ms * 1e-3) / 1e9
     clk = clk.summary()
     sm_mhz = clk["sm_mhz"] or 1900.0
-    # FP32 CUDA-core peak at the sampled clock: 152 SMs x 128 lanes x 2 flop
-    fp32_peak_tflops = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    # FP32 CUDA-core peak at the sampled clock: SMs x 128 lanes x 2 flop
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak_tflops = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
     lc_ms = stage_ms["linecot"] or ms
     lc_flops = PRODUCTS_PER_SITE["linecot"] * FLOP_PER_PRODUCT * V
     lc_tflops = lc_flops / (lc_ms * 1e-3) / 1e12
@@ -636,9 +669,19 @@ def main():
         "stages_ms": stage_ms,
         "forward_only": {"value": wsz * V / (ms_fwd * 1e-3), "unit": "sites/s", "ms_per_step": ms_fwd,
                          "steps": nfwd, "what": "flue_magnetic: B^2 without the gradient (the reference's magnetic)"},
+        "forward_only_fp64": {"value": wsz * V / (ms_fwd64 * 1e-3), "unit": "sites/s", "ms_per_step": ms_fwd64,
+                              "steps": args.fp64_steps,
+                              "what": "flue_magnetic on the complex128 field: the reference's magnetic() at its own "
+                                      "precision, the same work as the CPU figures"},
         "gpu_launches": int(n_launches),
         "e2e": {"value": e2e_val, "unit": "sites/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d + 8,
-                "s_per_step": e2e_s, "api": "flue_magnetic_force_c (host complex64 in, host gradient out)"},
+                "s_per_step": e2e_s,
+                "api": f"flue_magnetic_force_c (host complex128 field in, {args.prec} FP32 compute, host complex128 "
+                       "gradient out)"},
+        "e2e_c64": {"value": wsz * V / e2e64_s, "unit": "sites/s", "h2d_bytes_per_step": h2d64,
+                    "d2h_bytes_per_step": h2d64 + 8, "s_per_step": e2e64_s,
+                    "api": f"flue_magnetic_force_c (host complex64 field in, {args.prec} FP32 compute, host "
+                           "complex64 gradient out)"},
         "roofline": {"bound": "hbm", "kernel": "whole fwd+bwd step (metric's %HBM)", "achieved": achieved_gbs,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
                      "traffic": step_traffic(args.prec, dims),
@@ -647,7 +690,8 @@ def main():
                              "achieved": lc_tflops, "peak": fp32_peak_tflops, "unit": "TFLOP/s",
                              "frac": lc_tflops / fp32_peak_tflops,
                              "step_tflops": step_flops / (ms * 1e-3) / 1e12,
-                             "peak_basis": "152 SM x 128 FP32 lanes x 2 flop x median sampled SM clock"},
+                             "peak_basis": f"{sm_count} SM x 128 FP32 lanes x 2 flop x median sampled SM clock"},
+        "sm_count": sm_count,
         "clocks": clk,
         "cpu_baseline": cpu,
     }

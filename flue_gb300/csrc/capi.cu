@@ -85,11 +85,11 @@ PlaneSet all_planes() {
 size_t ws_bytes_for(int op, const Geom& g, int prec) {
     switch (op) {
         case FLUE_OP_PLAQUETTE:
-            return a256((size_t)plaquette_blocks(g) * 8);
+            return a256((size_t)plaquette_slots(g) * 8);
         case FLUE_OP_POLYAKOV:
-            return a256((size_t)polyakov_blocks(g) * 16);
+            return a256((size_t)polyakov_slots(g) * 16);
         case FLUE_OP_WMUNU:
-            return a256((size_t)wloop_blocks(g) * 8);
+            return a256((size_t)wloop_slots(g) * 8);
         case FLUE_OP_FMUNU: {
             PlaneSet ps;
             ps.np = 1;
@@ -106,7 +106,7 @@ size_t ws_bytes_for(int op, const Geom& g, int prec) {
         case FLUE_OP_PLAQUETTE_FORCE:
             return a256((size_t)plaqforce_blocks(g) * 4 * 8);
         case FLUE_OP_MEANLINK:
-            return a256((size_t)meanlink_blocks(g) * 4 * 8);
+            return a256((size_t)meanlink_slots(g) * 4 * 8);
         case FLUE_OP_WFLOW:
             return wflow_ws_bytes(g);
         case FLUE_OP_GLUON_PROP:

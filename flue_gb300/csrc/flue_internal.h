@@ -49,8 +49,21 @@ cudaError_t launch_unpack(const FieldRef& U, void* dst, int dst_dtype, cudaStrea
 cudaError_t launch_matmul_batch(const void* l, const void* r, void* o, int64_t n, int dtype, int dagger, cudaStream_t st);
 cudaError_t launch_fix_field(void* links, const Geom& g, int prec, cudaStream_t st);
 
-// observables.  Partial-sum scratch `part` needs partial_slots(...) doubles.
+// SM count of the current device (cudaDevAttrMultiProcessorCount), looked up
+// once per device; 152 when no device answers (host-only size queries)
+int device_sms();
+// upper bound of every reduction grid below: 4 blocks per SM for up to 256
+// SMs.  Workspaces hold this many partial-sum slots (the *_slots sizes), so
+// a workspace sized on one device fits the grid on any other.
+constexpr int kMaxRedBlocks = 1024;
+
+// observables.  *_blocks is the launch grid on the current device (<=
+// kMaxRedBlocks); the partial-sum scratch `part` needs *_slots(...) entries.
 int plaquette_blocks(const Geom& g);
+int plaquette_slots(const Geom& g);
+int polyakov_slots(const Geom& g);
+int wloop_slots(const Geom& g);
+int meanlink_slots(const Geom& g);
 cudaError_t launch_plaquette(const FieldRef& U, int mu0, int mu1, int nu1, double* part, double* out, cudaStream_t st);
 int polyakov_blocks(const Geom& g);
 cudaError_t launch_polyakov(const FieldRef& U, double* part, double* out2, cudaStream_t st);

@@ -7,6 +7,8 @@
 // per block with warp shuffles, and finished by a one-block kernel that adds
 // the block partials in index order, so results are bitwise reproducible for
 // a given lattice size.
+#include <atomic>
+
 #include "flue_internal.h"
 
 namespace flue {
@@ -16,6 +18,30 @@ static inline int grid_for(int64_t n, int bs, int cap) {
     if (b > cap) b = cap;
     if (b < 1) b = 1;
     return (int)b;
+}
+
+int device_sms() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 152;
+    }
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        return 152;
+    }
+    cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
+// Grid-strided reductions run 4 blocks per SM of the current device, at most
+// kMaxRedBlocks; their partial-sum workspaces are sized for kMaxRedBlocks.
+static int red_cap() {
+    const int c = 4 * device_sms();
+    return c > kMaxRedBlocks ? kMaxRedBlocks : c;
 }
 
 // ---------------------------------------------------------------------------
@@ -228,7 +254,8 @@ cudaError_t launch_matmul_batch(const void* l, const void* r, void* o, int64_t n
 // ---------------------------------------------------------------------------
 constexpr int RED_BS = 256;
 
-int plaquette_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
+int plaquette_blocks(const Geom& g) { return grid_for(g.V, RED_BS, red_cap()); }
+int plaquette_slots(const Geom& g) { return grid_for(g.V, RED_BS, kMaxRedBlocks); }
 
 // FP32: at most 128 registers (two 256-thread blocks per SM): measured on
 // GB300 at 32^3x64, all planes, c64 0.53 -> 0.36 ms per call against the
@@ -287,8 +314,9 @@ cudaError_t launch_plaquette(const FieldRef& U, int mu0, int mu1, int nu1, doubl
 // thread per spatial site walks its column (the tree issues ~3x the FP64
 // products per site and the FP64 pipe is the bound: 32^3x64 0.53 ms serial
 // against 1.11 ms as a tree; FP32 0.17 -> 0.13 ms per call as a tree).
-static int polyakov_blocks_serial(const Geom& g) { return grid_for(g.V / g.n[0], RED_BS, 4 * 152); }
-int polyakov_blocks(const Geom& g) { return grid_for(g.V / g.n[0], RED_BS / 32, 4 * 152); }  // the larger grid
+static int polyakov_blocks_serial(const Geom& g) { return grid_for(g.V / g.n[0], RED_BS, red_cap()); }
+int polyakov_blocks(const Geom& g) { return grid_for(g.V / g.n[0], RED_BS / 32, red_cap()); }
+int polyakov_slots(const Geom& g) { return grid_for(g.V / g.n[0], RED_BS / 32, kMaxRedBlocks); }  // the larger grid
 
 template <typename T>
 __device__ __forceinline__ M3<T> shfl_down_m3(const M3<T>& m, int off) {
@@ -356,7 +384,8 @@ cudaError_t launch_polyakov(const FieldRef& U, double* part, double* out2, cudaS
 // nMu x nNu Wilson loop at every site (tau < 0) or on the slice t = tau
 // (src/wloops.F90:599-675 and :711-789).
 // ---------------------------------------------------------------------------
-int wloop_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
+int wloop_blocks(const Geom& g) { return grid_for(g.V, RED_BS, red_cap()); }
+int wloop_slots(const Geom& g) { return grid_for(g.V, RED_BS, kMaxRedBlocks); }
 
 // coordinate, extent and stride of direction d (runtime) without
 // runtime-indexed arrays (they would go to local memory)
@@ -581,7 +610,8 @@ cudaError_t launch_genericpath(const FieldRef& U, const int* path_host, int npat
 // Landau-gauge mean link: per direction sum over sites of
 // Re Tr(G(x) U_mu(x) G(x+mu)^+), G in (NT,NX,NY,NZ,3,3) layout.
 // ---------------------------------------------------------------------------
-int meanlink_blocks(const Geom& g) { return grid_for(g.V, RED_BS, 4 * 152); }
+int meanlink_blocks(const Geom& g) { return grid_for(g.V, RED_BS, red_cap()); }
+int meanlink_slots(const Geom& g) { return grid_for(g.V, RED_BS, kMaxRedBlocks); }
 
 template <typename T, typename G2>
 __device__ __forceinline__ M3<T> load_g(const G2* __restrict__ G, int64_t V, int64_t s) {

@@ -60,7 +60,7 @@ def lib():
                 "oracle_genplaquette": ([P, I, I, I, I, I, I, I, I, P, P], None),
                 "oracle_plaquette": ([P, I, I, I, I, I, I, I, P, P], None),
                 "oracle_polyakov": ([P, I, I, I, I, P, P], I),
-                "oracle_wmunu": ([P, I, I, I, I, I, I, I, I], D),
+                "oracle_wmunu": ([P, I, I, I, I, I, I, I, I, I], D),
                 "oracle_wmunutau": ([P, I, I, I, I, I, I, I, I, I], D),
                 "oracle_clover": ([P, I, I, I, I, I, I, P], None),
                 "oracle_loop5": ([P, I, I, I, I, I, I, P], None),
@@ -165,9 +165,9 @@ def polyakov(data):
     return s.value, n.value
 
 
-def wmunu(data, mu, nu, nmu, nnu):
+def wmunu(data, mu, nu, nmu, nnu, parallel=False):
     a = _fortran_field(data)
-    return lib().oracle_wmunu(_ptr(a), *_dims(a), mu, nu, nmu, nnu)
+    return lib().oracle_wmunu(_ptr(a), *_dims(a), mu, nu, nmu, nnu, int(bool(parallel)))
 
 
 def wmunutau(data, tau, mu, nu, nmu, nnu):

@@ -442,10 +442,24 @@ static double wloop_site(const field *f, const int base[4], int mu, int nu, int 
     return rtracemm(&a, &b);
 }
 
-double oracle_wmunu(const double *data, int nt, int nx, int ny, int nz, int mu, int nu, int nmu, int nnu) {
+/* parallel != 0: the same per-site loops under an OpenMP reduction (only the
+ * order of the FP64 sum over sites differs), for full-size lattices. */
+double oracle_wmunu(const double *data, int nt, int nx, int ny, int nz, int mu, int nu, int nmu, int nnu,
+                    int parallel) {
     field f;
     init_field(&f, data, nt, nx, ny, nz);
     double v = 0.0;
+    if (parallel) {
+#pragma omp parallel for collapse(4) reduction(+ : v) schedule(static)
+        for (int x = 1; x <= nx; ++x)
+            for (int y = 1; y <= ny; ++y)
+                for (int z = 1; z <= nz; ++z)
+                    for (int t = 1; t <= nt; ++t) {
+                        int base[4] = {t, x, y, z};
+                        v += wloop_site(&f, base, mu, nu, nmu, nnu);
+                    }
+        return v / (double)f.V;
+    }
     for (int x = 1; x <= nx; ++x)
         for (int y = 1; y <= ny; ++y)
             for (int z = 1; z <= nz; ++z)
