@@ -759,8 +759,8 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
         if (!d_grad) continue;
         if ((e = cudaStreamWaitEvent(c->s_out, c->ev_cp[j], 0)) != cudaSuccess) break;
         const unsigned ob = k == nslab - 1 ? 0u : out_blocks;
-        if ((e = launch_energy_slab_out(U, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, ob, c->s_out)) !=
-            cudaSuccess)
+        if ((e = launch_energy_slab_out(U, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, ob, c->s_out,
+                                        data_dtype)) != cudaSuccess)
             break;
         if ((e = cudaEventRecord(c->ev_out[j], c->s_out)) != cudaSuccess) break;
     }
@@ -995,8 +995,8 @@ int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int 
     if (!data || !B) return fail(FLUE_ERR_ARG, "NULL pointer");
     if (data_dtype != FLUE_C128 && data_dtype != FLUE_C64) return fail(FLUE_ERR_DTYPE, "data must be c128 or c64");
     if (!prec_ok(prec)) return fail(FLUE_ERR_DTYPE, "bad precision");
-    if ((data_dtype == FLUE_C128) != (prec == FLUE_C128))
-        return fail(FLUE_ERR_DTYPE, "c128 data needs FLUE_C128, c64 data FLUE_C64 or FLUE_R12");
+    if (data_dtype == FLUE_C64 && prec == FLUE_C128)
+        return fail(FLUE_ERR_DTYPE, "c64 data is computed in FLUE_C64 or FLUE_R12");
     if (!dims_ok(NT, NX, NY, NZ)) return fail(FLUE_ERR_SHAPE, "bad lattice extents");
     HOST_PROLOGUE();
     const size_t in_bytes = (size_t)flue_field_bytes(NT, NX, NY, NZ, data_dtype);
@@ -1015,6 +1015,9 @@ int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int 
             return magnetic_force_pipelined(c, d_in, data_dtype, NT, NX, NY, NZ, prec, force_form, B, d_grad, nslab);
     }
     flue_field U = {nullptr, NT, NX, NY, NZ, prec};
+    // a complex128 field computed in FP32 (c128 data, prec C64 / R12) gets
+    // its FP32 gradient widened back to complex128 before it leaves the GPU
+    const bool widen = data_dtype == FLUE_C128 && prec != FLUE_C128;
     if (d_in) {
         const size_t fb = (size_t)flue_field_bytes(NT, NX, NY, NZ, prec);
         if ((rc = grow(&c->field2, &c->field2_bytes, fb))) return rc;
@@ -1025,23 +1028,36 @@ int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int 
         cudaError_t e = copy_async(c, c->field, data, in_bytes, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cuda_status(e);
         U.links = c->field;
-        if (prec == FLUE_R12) {
-            if ((rc = grow(&c->field2, &c->field2_bytes, (size_t)flue_field_bytes(NT, NX, NY, NZ, FLUE_R12)))) return rc;
-            if ((rc = flue_pack_field(c->field, FLUE_C64, st, NT, NX, NY, NZ, c->field2, FLUE_R12, 0, c->st))) return rc;
+        if (prec != data_dtype) {
+            if ((rc = grow(&c->field2, &c->field2_bytes, (size_t)flue_field_bytes(NT, NX, NY, NZ, prec)))) return rc;
+            if ((rc = flue_pack_field(c->field, data_dtype, st, NT, NX, NY, NZ, c->field2, prec, 0, c->st))) return rc;
             U.links = c->field2;
         }
     }
     if ((rc = ensure_ws(c, FLUE_OP_MAGNETIC_FORCE, U))) return rc;
     void* force_out = nullptr;
+    void* grad_dst = nullptr;  // where the gradient in the data's dtype ends up on the device
     if (grad) {
         if (d_grad) {
-            force_out = d_grad;
+            grad_dst = d_grad;
         } else {
             if ((rc = grow(&c->out, &c->out_bytes, in_bytes))) return rc;
-            force_out = c->out;
+            grad_dst = c->out;
+        }
+        force_out = grad_dst;
+        if (widen) {
+            // FP32 gradient first, in c->field (its complex128 input has been
+            // packed into c->field2 by now), then widened into grad_dst
+            if ((rc = grow(&c->field, &c->field_bytes, (size_t)flue_field_bytes(NT, NX, NY, NZ, FLUE_C64)))) return rc;
+            force_out = c->field;
         }
     }
     if ((rc = flue_magnetic_force(&U, c->scal, force_out, force_form, c->ws, c->ws_bytes, c->st))) return rc;
+    if (grad && widen) {
+        const FieldRef G{force_out, make_geom(NT, NX, NY, NZ), FLUE_C64};
+        cudaError_t e = launch_unpack(G, grad_dst, FLUE_C128, c->st);
+        if (e != cudaSuccess) return cuda_status(e);
+    }
     if (grad && !d_grad) {
         cudaError_t e = copy_async(c, grad, c->out, in_bytes, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_status(e);

@@ -708,11 +708,23 @@ struct RefOut {
     // goes to site t0 + s % nts + ntf * (s / nts) of the full lattice, whose
     // time extent is ntf and volume V.  nts = 0: site s is site s.
     int nts = 0, ntf = 0, t0 = 0;
+    // complex128 destination of an FP32 computation (p unused when set): the
+    // gradient of a complex128 field computed in FP32 is written back in the
+    // field's own dtype
+    double2* __restrict__ pd = nullptr;
     __device__ __forceinline__ void store(int64_t s, int slot, const M3<T>& m) const {
         const int64_t sf = nts ? (int64_t)t0 + s % nts + (int64_t)ntf * (s / nts) : s;
         if (!FLUE_INB(sf >= 0 && sf < V && slot >= 0 && slot < nslot)) return;
-        C2* q = p + sf + V * slot;
         const int64_t st = V * nslot;
+        if (pd) {
+            double2* q = pd + sf + V * slot;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) q[st * (a + 3 * b)] = make_double2(m.r[3 * a + b], m.i[3 * a + b]);
+            return;
+        }
+        C2* q = p + sf + V * slot;
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll

@@ -681,16 +681,19 @@ cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const Pla
 }
 
 cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
-                                   int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st) {
+                                   int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st,
+                                   int out_dtype) {
     if (has_time_plane(ps) || vfull < U.g.V || t0 < 0 || t0 + U.g.n[0] > ntf) return cudaErrorInvalidValue;
     const PlaneArg pa = make_planes(ps);
     const EnergyWs w = energy_layout(U.g, U.prec, pa, true);
     if (ws_bytes < w.total) return cudaErrorInvalidValue;
     if (U.prec == PREC_C128) {
+        if (out_dtype != PREC_C128) return cudaErrorInvalidValue;
         RefOut<double> fo{(double2*)force, vfull, 4, U.g.n[0], ntf, t0};
         return energy_out_part<double>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
     }
     RefOut<float> fo{(float2*)force, vfull, 4, U.g.n[0], ntf, t0};
+    if (out_dtype == PREC_C128) fo.p = nullptr, fo.pd = (double2*)force;
     return energy_out_part<float>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
 }
 
@@ -782,7 +785,8 @@ cudaError_t launch_energy_slabs(const FieldRef& U, const PlaneSet& ps, double* o
         e = launch_energy_slab_fwd(U, t0, n, ps, U.g.V, spart ? spart + k : nullptr, with_force, slot, w.slot, sk);
         if (e == cudaSuccess && with_force) {
             const FieldRef Us{U.links, make_geom(n, U.g.n[1], U.g.n[2], U.g.n[3]), U.prec};
-            e = launch_energy_slab_out(Us, ps, U.g.V, U.g.n[0], t0, force, form, slot, w.slot, 0, sk);
+            e = launch_energy_slab_out(Us, ps, U.g.V, U.g.n[0], t0, force, form, slot, w.slot, 0, sk,
+                                       U.prec == PREC_C128 ? PREC_C128 : PREC_C64);
         }
     }
     // join every library stream back into the caller's stream, also on error

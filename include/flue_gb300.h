@@ -312,7 +312,9 @@ int flue_uzerobar_c(const double *data, int NT, int NX, int NY, int NZ, const do
 int flue_scalargluonprop_c(int NS, int NT, const void *U, double xi, double *D);
 /* B^2 forward + backward from host buffers: data is complex128
  * (data_dtype FLUE_C128) or complex64 (FLUE_C64), computed in precision
- * prec; grad (host, same layout and dtype as data) receives the gradient
+ * prec -- complex128 data in any precision (FP32 link products for FLUE_C64
+ * and FLUE_R12, the field rounded on the GPU), complex64 data in FLUE_C64 or
+ * FLUE_R12; grad (host, same layout and dtype as data) receives the gradient
  * of B^2 in form force_form. */
 int flue_magnetic_force_c(const void *data, int data_dtype, int NT, int NX, int NY, int NZ, int prec, int force_form,
                           double *B, void *grad);

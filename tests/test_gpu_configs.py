@@ -102,15 +102,15 @@ def test_config0_fp32_every_observable(U0, grad0, prec):
     so, no = oracle.polyakov(U)
     assert abs(s - so) < 1e-6 * n
     for path in PATHS:
-        assert np.abs(_np(G.genericpath_all(f, path)) - oracle.genericpath_all(U, path)).max() < 3e-6
+        assert np.abs(_np(G.genericpath_all(f, path)) - oracle.genericpath_all(U, path)).max() < 2e-6
     tab = _np(G.wmunu_table(f, 2, 3, 8, 8))
     for r, t in ((0, 0), (3, 5), (7, 7)):
         assert abs(tab[r, t] - oracle.wmunu(U, 2, 3, r + 1, t + 1)) < 2e-6, (r, t)
     for mu, nu in ALL_PLANES:
         c = oracle.cloverloopmunucoord(U, mu, nu)
-        assert np.abs(_np(G.cloverloopmunucoord(f, mu, nu)) - c).max() < 5e-6 * np.abs(c).max()
+        assert np.abs(_np(G.cloverloopmunucoord(f, mu, nu)) - c).max() < 2e-6 * np.abs(c).max()
         q = oracle.loop5munucoord(U, mu, nu)
-        assert np.abs(_np(G.loop5munucoord(f, mu, nu)) - q).max() < 2e-5 * np.abs(q).max()
+        assert np.abs(_np(G.loop5munucoord(f, mu, nu)) - q).max() < 2e-6 * np.abs(q).max()
     bo = oracle.magnetic(U)
     assert rel(G.magnetic(f), bo) < FP32_BOUND
     b2, grad = forces.magnetic_force(f)
@@ -157,8 +157,8 @@ def test_config1_size_haar_field():
     bo = oracle.magnetic(U, parallel=True)
     assert rel(G.magnetic(f), bo) < 1e-12
     a, b = G.uzerobar(f), oracle.uzerobar(U)
-    assert np.array_equal(np.isnan(a), np.isnan(b))
+    assert np.array_equal(np.isnan(a), np.isnan(b))  # a negative mean plaquette has no real root: NaN on both sides
     ok = ~np.isnan(b)
-    assert np.abs(a[ok] - b[ok]).max() < 1e-12
+    assert not ok.any() or np.abs(a[ok] - b[ok]).max() < 1e-12
     for prec in ("c64", "r12"):
         assert rel(G.magnetic(GaugeField.from_array(f, prec=prec)), bo) < FP32_BOUND, prec

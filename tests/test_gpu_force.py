@@ -96,7 +96,7 @@ def test_fp32_force_error_bound(prec):
     b32, g32 = forces.magnetic_force(GaugeField.from_array(U, prec=prec))
     g64, g32 = _np(g64), _np(g32).astype(np.complex128)
     assert abs(b32 - b64) / abs(b64) < 1e-6
-    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-5
+    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-6  # measured 2.2e-7 (c64, r12)
 
 
 @pytest.mark.parametrize("pinned", [True, False])
@@ -126,17 +126,20 @@ def test_host_buffer_force_entry(pinned):
         assert np.abs(g - _np(g_ref)).max() < 1e-5 * np.abs(_np(g_ref)).max()
 
 
-@pytest.mark.parametrize("prec_name", ["c64", "r12", "c128"])
-def test_host_buffer_force_time_slabs(prec_name, monkeypatch):
+@pytest.mark.parametrize("prec_name,data_name", [("c64", "c64"), ("r12", "c64"), ("c128", "c128"), ("r12", "c128"),
+                                                 ("c64", "c128")])
+def test_host_buffer_force_time_slabs(prec_name, data_name, monkeypatch):
     """The host-buffer force pipelined over time slabs (even, uneven and
     one-slice slabs) gives the gradient of the single-pass call bit for bit
-    and B^2 to FP64 summation order."""
+    and B^2 to FP64 summation order -- also for a complex128 field computed
+    in FP32, whose gradient comes back as complex128 and equals the device
+    FP32 gradient of the same field widened."""
     import ctypes
 
     from flue_gb300 import _lib
 
     U = generate.random_field((8, 4, 6, 4), 0.4, 10)
-    c128 = prec_name == "c128"
+    c128 = data_name == "c128"
     dt = np.complex128 if c128 else np.complex64
     host = torch.as_tensor(np.asfortranarray(U.astype(dt))).permute(6, 5, 4, 3, 2, 1, 0).contiguous().pin_memory()
     L = _lib.load()
@@ -154,6 +157,10 @@ def test_host_buffer_force_time_slabs(prec_name, monkeypatch):
 
     b1, g1 = run(1)
     assert np.isfinite(g1).all()
+    if c128 and prec_name != "c128":
+        bd, gd = forces.magnetic_force(GaugeField.from_array(U, prec=prec_name))
+        assert abs(b1 - bd) < 1e-12 * abs(bd)
+        assert np.array_equal(g1, _np(gd).astype(np.complex128).transpose(6, 5, 4, 3, 2, 1, 0))
     for slabs in (2, 3, 8):
         b, g = run(slabs)
         assert abs(b - b1) < 1e-12 * abs(b1), slabs

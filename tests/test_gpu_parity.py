@@ -154,16 +154,30 @@ def test_layouts_roundtrip():
     assert np.abs(back - U).max() < 5e-7
 
 
-@pytest.mark.parametrize("prec,tol", [("c64", 2e-6), ("r12", 3e-6)])
-def test_fp32_observables(prec, tol):
+# FP32 bounds (link products in FP32, sums in FP64), each a few times the
+# largest error measured on the GB300 over the parity lattices (4^4 to 16x8^3,
+# eps 0.3 to 0.8 and Haar, c64 and r12): B^2 3.7e-8 relative, gradient
+# 3.0e-7 relative L2 and 4.7e-7 of its largest element, plaquette 2.0e-8 and
+# Polyakov 2.7e-8 per term, genericPath 4.6e-7, W loops 9.3e-8, clover and
+# 5-loop F 3.2e-7 and 3.6e-7 of their largest element.
+FP32_B2 = 1e-6  # the headline's bound for B^2 and its gradient (relative L2)
+FP32_PER_TERM = 2e-7
+FP32_MATRIX = 2e-6
+
+
+@pytest.mark.parametrize("prec", ["c64", "r12"])
+def test_fp32_observables(prec):
     U = _field(((8, 4, 6, 4), 0.3, 9))
     f = GaugeField.from_array(U, prec=prec)
     for r in ((1, 4, 4), (2, 4, 4), (1, 1, 4)):
-        assert rel(G.plaquette(f, *r)[0], oracle.plaquette(U, *r)[0]) < tol
-    assert abs(G.polyakov(f)[0] - oracle.polyakov(U)[0]) < tol * 96
-    assert rel(G.magnetic(f), oracle.magnetic(U)) < 20 * tol
+        s, n, _ = G.plaquette(f, *r)
+        assert abs(s - oracle.plaquette(U, *r)[0]) < FP32_PER_TERM * n
+    s, n, _ = G.polyakov(f)
+    assert abs(s - oracle.polyakov(U)[0]) < FP32_PER_TERM * n
+    assert rel(G.magnetic(f), oracle.magnetic(U)) < FP32_B2
     a = G.loop5munucoord(f, 3, 2).cpu().numpy()
-    assert np.abs(a - oracle.loop5munucoord(U, 3, 2)).max() < 10 * tol
+    q = oracle.loop5munucoord(U, 3, 2)
+    assert np.abs(a - q).max() < FP32_MATRIX * np.abs(q).max()
 
 
 def _host(x):
@@ -181,36 +195,38 @@ def test_fp32_every_observable(U, prec):
     for r in ((1, 4, 4), (2, 4, 4), (1, 1, 4)):
         s, n, _ = G.plaquette(f, *r)
         so, no = oracle.plaquette(U, *r)
-        assert n == no and abs(s - so) < 1e-5 * n, r
+        assert n == no and abs(s - so) < FP32_PER_TERM * n, r
     if U.shape[0] >= 3:
         s, n, _ = G.polyakov(f)
         so, no = oracle.polyakov(U)
-        assert n == no and abs(s - so) < 3e-6 * U.shape[0] * n
+        assert n == no and abs(s - so) < FP32_PER_TERM * n
     for args in ((2, 3, 2, 1), (1, 4, 1, 2), (4, 2, 3, 3)):
-        assert abs(G.wmunu(f, *args) - oracle.wmunu(U, *args)) < 2e-5, args
-    assert abs(G.wmunutau(f, 1, 2, 4, 2, 1) - oracle.wmunutau(U, 1, 2, 4, 2, 1)) < 2e-5
+        assert abs(G.wmunu(f, *args) - oracle.wmunu(U, *args)) < 1e-6, args
+    assert abs(G.wmunutau(f, 1, 2, 4, 2, 1) - oracle.wmunutau(U, 1, 2, 4, 2, 1)) < 1e-6
     tab = _host(G.wmunu_table(f, 3, 4, 3, 2))
     for r in range(3):
         for t in range(2):
-            assert abs(tab[r, t] - oracle.wmunu(U, 3, 4, r + 1, t + 1)) < 2e-5, (r, t)
+            assert abs(tab[r, t] - oracle.wmunu(U, 3, 4, r + 1, t + 1)) < 1e-6, (r, t)
     path = [2, 3, -2, 4, -3, -4, 1, -1]
     gp = _host(G.genericpath(f, [1, 1, 1, 1], path))
-    assert np.abs(gp - oracle.genericpath(U, [1, 1, 1, 1], path)).max() < 1e-5
-    assert np.abs(_host(G.genericpath_all(f, path)) - oracle.genericpath_all(U, path)).max() < 1e-5
+    assert np.abs(gp - oracle.genericpath(U, [1, 1, 1, 1], path)).max() < FP32_MATRIX
+    assert np.abs(_host(G.genericpath_all(f, path)) - oracle.genericpath_all(U, path)).max() < FP32_MATRIX
     for mu, nu in ((1, 2), (3, 4)):
+        co = oracle.cloverloopmunucoord(U, mu, nu)
         c = _host(G.cloverloopmunucoord(f, mu, nu))
-        assert np.abs(c - oracle.cloverloopmunucoord(U, mu, nu)).max() < 1e-5, (mu, nu)
+        assert np.abs(c - co).max() < FP32_MATRIX * np.abs(co).max(), (mu, nu)
+        qo = oracle.loop5munucoord(U, mu, nu)
         q = _host(G.loop5munucoord(f, mu, nu))
-        assert np.abs(q - oracle.loop5munucoord(U, mu, nu)).max() < 5e-5, (mu, nu)
+        assert np.abs(q - qo).max() < FP32_MATRIX * np.abs(qo).max(), (mu, nu)
     b = G.magnetic(f)
     bo = oracle.magnetic(U)
-    assert abs(b - bo) < 1e-4 * max(1.0, abs(bo))
+    assert rel(b, bo) < FP32_B2
     b, g = forces.magnetic_force(f)
     g = _host(g).astype(np.complex128)
     go = oracle.loop5_energy_force(U, oracle.B2_PLANES)
-    assert abs(b - bo) < 1e-4 * max(1.0, abs(bo))
-    assert np.linalg.norm(g - go) < 5e-5 * np.linalg.norm(go)
-    assert np.abs(g - go).max() < 1e-4 * np.abs(go).max()
+    assert rel(b, bo) < FP32_B2
+    assert np.linalg.norm(g - go) < FP32_B2 * np.linalg.norm(go)
+    assert np.abs(g - go).max() < FP32_MATRIX * np.abs(go).max()
 
 
 # ---------------------------------------------------------------------------
