@@ -446,6 +446,31 @@ struct MatAoS<float> {
         for (int j = 0; j < 4; ++j) q[32 * j] = make_float4(m.r[2 * j], m.i[2 * j], m.r[2 * j + 1], m.i[2 * j + 1]);
         q[128] = make_float4(m.r[8], m.i[8], 0.f, 0.f);
     }
+    // 32-bit form of the address arithmetic, for buffers of fewer than 2^31
+    // float4 units (fits32): plane k starts k * pstride32() units in, site s
+    // of a plane (s >> 5) * 160 + (s & 31) units in
+    __device__ __forceinline__ uint32_t pstride32() const { return (uint32_t)((V + 31) >> 5) * 160u; }
+    __device__ __forceinline__ const float4* unit0_32(uint32_t s, int k) const {
+        return p + ((uint32_t)k * pstride32() + (s >> 5) * 160u + (s & 31u));
+    }
+    __device__ __forceinline__ M3<float> load32(uint32_t s, int k) const {
+        if (!ok((int64_t)s, k)) return m_zero<float>();
+        const float4* q = unit0_32(s, k);
+        M3<float> m;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 v = q[32 * j];
+            m.r[2 * j] = v.x;
+            m.i[2 * j] = v.y;
+            m.r[2 * j + 1] = v.z;
+            m.i[2 * j + 1] = v.w;
+        }
+        const float4 v = q[128];
+        m.r[8] = v.x;
+        m.i[8] = v.y;
+        return m;
+    }
+    static bool fits32(int64_t V, int64_t nk) { return (uint64_t)nk * (uint64_t)((V + 31) >> 5) * 160u < (1ull << 31); }
     static constexpr size_t bytes_per_matrix = 80;
     // bytes of nk planes over V sites (V rounded up to whole tiles)
     static size_t bytes(int64_t V, int64_t nk) { return (size_t)nk * (size_t)((V + 31) & ~(int64_t)31) * 80; }
@@ -476,6 +501,20 @@ struct MatAoS<double> {
 #pragma unroll
         for (int e = 0; e < 9; ++e) q[e] = make_double2(m.r[e], m.i[e]);
     }
+    // 32-bit form (fits32): matrix (k, s) at (k * V + s) * 9 double2 units
+    __device__ __forceinline__ M3<double> load32(uint32_t s, int k) const {
+        if (!ok((int64_t)s, k)) return m_zero<double>();
+        const double2* q = p + ((uint32_t)k * (uint32_t)V + s) * 9u;
+        M3<double> m;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            const double2 v = q[e];
+            m.r[e] = v.x;
+            m.i[e] = v.y;
+        }
+        return m;
+    }
+    static bool fits32(int64_t V, int64_t nk) { return (uint64_t)nk * (uint64_t)V * 9u < (1ull << 31); }
     static constexpr size_t bytes_per_matrix = 144;
     static size_t bytes(int64_t V, int64_t nk) { return (size_t)nk * (size_t)V * 144; }
 };
@@ -521,8 +560,8 @@ template <typename T>
 __device__ __forceinline__ T ahi(const T v[9], int a, int c) {  // Im K_ac
     return (a == c) ? v[a] : ((a + c) == 1) ? v[4] : ((a + c) == 2) ? v[6] : v[8];
 }
-// C += K X
-template <typename T>
+// C += K op(X), op = dagger when DX
+template <bool DX = false, typename T>
 __device__ __forceinline__ void mac_kx(M3<T>& C, const T k[9], const M3<T>& X) {
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -531,7 +570,8 @@ __device__ __forceinline__ void mac_kx(M3<T>& C, const T k[9], const M3<T>& X) {
             T re = C.r[3 * a + b], im = C.i[3 * a + b];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const T xr = X.r[3 * c + b], xi = X.i[3 * c + b];
+                const T xr = DX ? X.r[3 * b + c] : X.r[3 * c + b];
+                const T xi = DX ? -X.i[3 * b + c] : X.i[3 * c + b];
                 const T ki = ahi(k, a, c);
                 if (a != c) {
                     const T kr = ahr(k, a, c);
@@ -545,8 +585,8 @@ __device__ __forceinline__ void mac_kx(M3<T>& C, const T k[9], const M3<T>& X) {
             C.i[3 * a + b] = im;
         }
 }
-// C += X K
-template <typename T>
+// C += op(X) K, op = dagger when DX
+template <bool DX = false, typename T>
 __device__ __forceinline__ void mac_xk(M3<T>& C, const M3<T>& X, const T k[9]) {
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -555,7 +595,8 @@ __device__ __forceinline__ void mac_xk(M3<T>& C, const M3<T>& X, const T k[9]) {
             T re = C.r[3 * a + b], im = C.i[3 * a + b];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const T xr = X.r[3 * a + c], xi = X.i[3 * a + c];
+                const T xr = DX ? X.r[3 * c + a] : X.r[3 * a + c];
+                const T xi = DX ? -X.i[3 * c + a] : X.i[3 * a + c];
                 const T ki = ahi(k, c, b);
                 if (c != b) {
                     const T kr = ahr(k, c, b);
@@ -596,6 +637,19 @@ struct AHAoS<float> {
         v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
         v[8] = c.x;
     }
+    // 32-bit form (fits32)
+    __device__ __forceinline__ void load_packed32(uint32_t s, int k, float v[9]) const {
+        if (!ok((int64_t)s, k)) {
+            for (int e = 0; e < 9; ++e) v[e] = 0;
+            return;
+        }
+        const float4* q = p + ((uint32_t)k * ((uint32_t)((V + 31) >> 5) * 96u) + (s >> 5) * 96u + (s & 31u));
+        const float4 a = q[0], b = q[32], c = q[64];
+        v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w;
+        v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+        v[8] = c.x;
+    }
+    static bool fits32(int64_t V, int64_t nk) { return (uint64_t)nk * (uint64_t)((V + 31) >> 5) * 96u < (1ull << 31); }
     __device__ __forceinline__ M3<float> load(int64_t s, int k) const {
         if (!ok(s, k)) return m_zero<float>();
         float v[9];
@@ -630,6 +684,18 @@ struct AHAoS<double> {
         v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y, v[4] = c.x;
         v[5] = c.y, v[6] = d.x, v[7] = d.y, v[8] = e.x;
     }
+    // 32-bit form (fits32)
+    __device__ __forceinline__ void load_packed32(uint32_t s, int k, double v[9]) const {
+        if (!ok((int64_t)s, k)) {
+            for (int e = 0; e < 9; ++e) v[e] = 0;
+            return;
+        }
+        const double2* q = p + ((uint32_t)k * (uint32_t)V + s) * 5u;
+        const double2 a = q[0], b = q[1], c = q[2], d = q[3], e = q[4];
+        v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y, v[4] = c.x;
+        v[5] = c.y, v[6] = d.x, v[7] = d.y, v[8] = e.x;
+    }
+    static bool fits32(int64_t V, int64_t nk) { return (uint64_t)nk * (uint64_t)V * 5u < (1ull << 31); }
     __device__ __forceinline__ M3<double> load(int64_t s, int k) const {
         if (!ok(s, k)) return m_zero<double>();
         const double2* q = p + ((int64_t)k * V + s) * 5;

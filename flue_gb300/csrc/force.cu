@@ -30,6 +30,8 @@
 //   4. link cotangents N_d(z) from the line cotangents of the lines through
 //      the link, then the su(3)-projected gradient G = -1/2 TA(U N) or the
 //      Euclidean gradient N^+                              (k_linkcot)
+#include <stdlib.h>
+
 #include <mutex>
 
 #include "flue_internal.h"
@@ -93,15 +95,6 @@ __device__ __forceinline__ int wrapd(int c, int k, int n) {
     return t - c;
 }
 
-// FLUE_LINES_DAG = 1 keeps daggered copies of the lines so that the line
-// cotangents need no select instructions for S3, S4 (twice the line storage).
-// Measured on GB300 at 32^3x64 with the tiled intermediates: k_lines 0.27 ->
-// 0.50 ms, k_linecot 7.22 -> 6.84 ms, the 16-slab step 10.46 -> 10.21 ms (with
-// the earlier 80-byte-stride layout the extra line writes cost more than the
-// selects saved).
-#ifndef FLUE_LINES_DAG
-#define FLUE_LINES_DAG 1
-#endif
 
 // Traversal order of the site blocks of the stencil kernels.  The lattice is
 // a sequence of rows (fixed y, z) of NT*NX sites.  When a row holds a whole
@@ -233,7 +226,7 @@ __device__ __forceinline__ Ctx<T> make_ctx(const MatAoS<T>& lines, const Geom& g
 //    never step in time then).
 // ---------------------------------------------------------------------------
 template <class L, typename T>
-__global__ void k_lines(L U, Geom g, Geom gs, int t0, PlaneArg pa, MatAoS<T> lines, int dag_copies) {
+__global__ void k_lines(L U, Geom g, Geom gs, int t0, PlaneArg pa, MatAoS<T> lines) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.V) return;
     const int slot = blockIdx.y;
@@ -254,15 +247,26 @@ __global__ void k_lines(L U, Geom g, Geom gs, int t0, PlaneArg pa, MatAoS<T> lin
     lines.store(s, 3 * slot + 1, l2);
     const M3<T> l3 = mul(l2, U.load(s2, d));
     lines.store(s, 3 * slot + 2, l3);
-#if FLUE_LINES_DAG
-    // daggered copies after the 3 * nd plain lines (the line cotangents read
-    // S3, S4 = L^+ without select instructions; only they use the copies)
-    if (dag_copies) {
-        lines.store(s, 3 * (pa.nd + slot), dag(u0));
-        lines.store(s, 3 * (pa.nd + slot) + 1, dag(l2));
-        lines.store(s, 3 * (pa.nd + slot) + 2, dag(l3));
-    }
-#endif
+}
+
+// Loads through 32-bit (I = uint32_t) or 64-bit (I = int64_t) address
+// arithmetic; the 32-bit form is used when every buffer the kernel indexes
+// has fewer than 2^31 vector units (MatAoS / AHAoS fits32).
+template <typename T>
+__device__ __forceinline__ M3<T> ldm(const MatAoS<T>& m, uint32_t s, int k) {
+    return m.load32(s, k);
+}
+template <typename T>
+__device__ __forceinline__ M3<T> ldm(const MatAoS<T>& m, int64_t s, int k) {
+    return m.load(s, k);
+}
+template <typename T>
+__device__ __forceinline__ void ldk(const AHAoS<T>& m, uint32_t s, int k, T v[9]) {
+    m.load_packed32(s, k, v);
+}
+template <typename T>
+__device__ __forceinline__ void ldk(const AHAoS<T>& m, int64_t s, int k, T v[9]) {
+    m.load_packed(s, k, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -299,7 +303,7 @@ struct MinBlocks<float> {
 };
 constexpr int FWD_BS = FLUE_FWD_BS;
 
-template <typename T>
+template <typename T, typename I>
 __global__ void __launch_bounds__(FWD_BS, MinBlocks<T>::fwd)
     k_fwd(Geom g, PlaneArg pa, int kind, PatchArg pt, MatAoS<T> lines, AHAoS<T> kout, RefOut<T> fout, double* part) {
     __shared__ double sh[32];
@@ -329,26 +333,29 @@ __global__ void __launch_bounds__(FWD_BS, MinBlocks<T>::fwd)
             const int a = shp[k].a, b = shp[k].b;
             const int km = cx.kmu + a - 1, kn = cx.knu + b - 1;
             // the 3 x 3 sites (i, j) in {-a, 0, a} x {-b, 0, b} the leaves use
+            // (site offsets within the lattice are 32-bit; the address
+            // arithmetic is 32-bit too when I = uint32_t)
             const int s0 = (int)cx.s, stm = (int)cx.stm, stn = (int)cx.stn;
             const int mM = wrapd(cx.cm, -a, cx.nm) * stm, mP = wrapd(cx.cm, a, cx.nm) * stm;
             const int nM = wrapd(cx.cn, -b, cx.nn) * stn, nP = wrapd(cx.cn, b, cx.nn) * stn;
+            auto ld = [&](int site, int k) { return ldm(lines, (I)site, k); };
             M3<T> w;
             {
-                const M3<T> m00 = lines.load(s0, km);
-                const M3<T> n00 = lines.load(s0, kn);
-                M3<T> t = mm<false, false>(m00, lines.load(s0 + mP, kn));
-                t = mm<false, true>(t, lines.load(s0 + nP, km));
+                const M3<T> m00 = ld(s0, km);
+                const M3<T> n00 = ld(s0, kn);
+                M3<T> t = mm<false, false>(m00, ld(s0 + mP, kn));
+                t = mm<false, true>(t, ld(s0 + nP, km));
                 w = mm<false, true>(t, n00);  // TR
-                const M3<T> ma0 = lines.load(s0 + mM, km);
-                t = mm<false, true>(n00, lines.load(s0 + mM + nP, km));
-                t = mm<false, true>(t, lines.load(s0 + mM, kn));
+                const M3<T> ma0 = ld(s0 + mM, km);
+                t = mm<false, true>(n00, ld(s0 + mM + nP, km));
+                t = mm<false, true>(t, ld(s0 + mM, kn));
                 mac<false, false>(w, t, ma0);  // TL
-                const M3<T> n0b = lines.load(s0 + nM, kn);
-                t = mm<true, true>(ma0, lines.load(s0 + mM + nM, kn));
-                t = mm<false, false>(t, lines.load(s0 + mM + nM, km));
+                const M3<T> n0b = ld(s0 + nM, kn);
+                t = mm<true, true>(ma0, ld(s0 + mM + nM, kn));
+                t = mm<false, false>(t, ld(s0 + mM + nM, km));
                 mac<false, false>(w, t, n0b);  // BL
-                t = mm<true, false>(n0b, lines.load(s0 + nM, km));
-                t = mm<false, false>(t, lines.load(s0 + mP + nM, kn));
+                t = mm<true, false>(n0b, ld(s0 + nM, km));
+                t = mm<false, false>(t, ld(s0 + mP + nM, kn));
                 mac<false, true>(w, t, m00);  // BR
             }
             m_axpy(q, (T)shp[k].c, w);
@@ -365,98 +372,288 @@ __global__ void __launch_bounds__(FWD_BS, MinBlocks<T>::fwd)
 }
 
 // ---------------------------------------------------------------------------
+// 2b. forward with the lines staged in shared memory per timeslice tile
+//     (FP32 5-loop energies over spatial planes; fwd_tile_ok).  A block
+//     of 128 threads covers FT_TT = 2 time slices x an 8 x 8 patch of the
+//     plane (mu, nu) at one value of the third spatial coordinate.  For each
+//     shape (a, b) the mu-lines of length a over the patch widened by a
+//     below in mu and by b on both sides in nu, and the nu-lines of length b
+//     over the patch widened by a on both sides in mu and by b below in nu,
+//     are copied into shared memory with cp.async (16 bytes per copy, the
+//     next shape's lines in flight while the current shape is computed,
+//     double buffered); the four leaves of each site then read their twelve
+//     lines from shared memory with 32-bit addresses.
+// ---------------------------------------------------------------------------
+constexpr int FT_TT = 2, FT_TM = 8, FT_TN = 8, FT_BS = FT_TT * FT_TM * FT_TN;
+// matrices of the largest shape's staging area, (3,3): 2 x 11 x 14 x 2
+constexpr int FT_MAXPOS = 2 * (FT_TM + 3) * (FT_TN + 6) * FT_TT;
+constexpr size_t FT_SMEM = 2 * (size_t)FT_MAXPOS * 5 * sizeof(float4);
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ M3<float> lds_mat(const float4* q) {
+    M3<float> m;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float4 v = q[j];
+        m.r[2 * j] = v.x;
+        m.i[2 * j] = v.y;
+        m.r[2 * j + 1] = v.z;
+        m.i[2 * j + 1] = v.w;
+    }
+    const float4 v = q[4];
+    m.r[8] = v.x;
+    m.i[8] = v.y;
+    return m;
+}
+
+struct TileGeom {
+    int nm, nn, stm, stn, sto;  // extents and site strides along mu, nu; stride of the third direction
+};
+
+__global__ void __launch_bounds__(FT_BS, 2)
+    k_fwd_tile(Geom g, PlaneArg pa, MatAoS<float> lines, AHAoS<float> kout, double* part) {
+    extern __shared__ float4 ft_sm[];
+    __shared__ double sh[32];
+    const int p = blockIdx.x % pa.np;
+    const int mu = sel(pa.mu, p), nu = sel(pa.nu, p), od = 6 - mu - nu;
+    TileGeom tg{1, 1, 0, 0, 0};
+#pragma unroll
+    for (int d = 1; d < 4; ++d) {
+        if (d == mu) tg.nm = g.n[d], tg.stm = (int)g.st[d];
+        if (d == nu) tg.nn = g.n[d], tg.stn = (int)g.st[d];
+        if (d == od) tg.sto = (int)g.st[d];
+    }
+    int r = blockIdx.x / pa.np;
+    const int ntb = g.n[0] / FT_TT, nmb = tg.nm / FT_TM, nnb = tg.nn / FT_TN;
+    const int tb = r % ntb;
+    r /= ntb;
+    const int mb = r % nmb;
+    r /= nmb;
+    const int nb = r % nnb;
+    const int oc = r / nnb;
+    const int t0 = tb * FT_TT, m0 = mb * FT_TM, n0 = nb * FT_TN, obase = oc * tg.sto;
+    const int tid = threadIdx.x;
+    const int tl = tid % FT_TT, ml = (tid / FT_TT) % FT_TM, nl = tid / (FT_TT * FT_TM);
+    const int kmu = 3 * sel(pa.slot, mu), knu = 3 * sel(pa.slot, nu);
+
+    // issue the copies of shape k's lines into buf (one commit group)
+    auto stage = [&](int k, float4* buf) {
+        const int a = c_shapes5[k].a, b = c_shapes5[k].b;
+        const int Wm = FT_TN + 2 * b, Rm = (FT_TM + a) * Wm * FT_TT;
+        const int Wn = FT_TN + b, Rn = (FT_TM + 2 * a) * Wn * FT_TT;
+        // exact quotient by W for the row numbers met here (< 256; W <= 14)
+        const unsigned invm = (65536u + Wm - 1) / Wm, invn = (65536u + Wn - 1) / Wn;
+        for (int pos = tid; pos < Rm + Rn; pos += FT_BS) {
+            const bool isn = pos >= Rm;
+            const int q = isn ? pos - Rm : pos;
+            const int W = isn ? Wn : Wm;
+            const int tt = q % FT_TT, rr = q / FT_TT;
+            const int im = (int)(((unsigned)rr * (isn ? invn : invm)) >> 16);
+            const int jn = rr - im * W;
+            int cm = m0 + im - a;
+            cm += cm < 0 ? tg.nm : 0;
+            cm -= cm >= tg.nm ? tg.nm : 0;
+            int cn = n0 + jn - b;
+            cn += cn < 0 ? tg.nn : 0;
+            cn -= cn >= tg.nn ? tg.nn : 0;
+            const uint32_t site = (uint32_t)(t0 + tt + cm * tg.stm + cn * tg.stn + obase);
+            const float4* src = lines.unit0_32(site, isn ? knu + b - 1 : kmu + a - 1);
+            float4* dst = buf + pos * 5;
+#pragma unroll
+            for (int u = 0; u < 5; ++u) cp_async16(dst + u, src + 32 * u);
+        }
+        cp_async_commit();
+    };
+
+    M3<float> q = m_zero<float>();
+    stage(0, ft_sm);
+#pragma unroll 1
+    for (int k = 0; k < 7; ++k) {
+        const float4* cur = ft_sm + (k & 1) * FT_MAXPOS * 5;
+        if (k + 1 < 7) {
+            stage(k + 1, ft_sm + ((k + 1) & 1) * FT_MAXPOS * 5);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const int a = c_shapes5[k].a, b = c_shapes5[k].b;
+        const int Wm = FT_TN + 2 * b, Rm = (FT_TM + a) * Wm * FT_TT, Wn = FT_TN + b;
+        // L(i, j): the line at offset (i mu + j nu) from the thread's site
+        auto Lm = [&](int i, int j) { return lds_mat(cur + (((ml + i + a) * Wm + nl + j + b) * FT_TT + tl) * 5); };
+        auto Ln = [&](int i, int j) {
+            return lds_mat(cur + (Rm + ((ml + i + a) * Wn + nl + j + b) * FT_TT + tl) * 5);
+        };
+        M3<float> w;
+        {
+            const M3<float> m00 = Lm(0, 0);
+            const M3<float> n00 = Ln(0, 0);
+            M3<float> t = mm<false, false>(m00, Ln(a, 0));
+            t = mm<false, true>(t, Lm(0, b));
+            w = mm<false, true>(t, n00);  // TR
+            const M3<float> ma0 = Lm(-a, 0);
+            t = mm<false, true>(n00, Lm(-a, b));
+            t = mm<false, true>(t, Ln(-a, 0));
+            mac<false, false>(w, t, ma0);  // TL
+            const M3<float> n0b = Ln(0, -b);
+            t = mm<true, true>(ma0, Ln(-a, -b));
+            t = mm<false, false>(t, Lm(-a, -b));
+            mac<false, false>(w, t, n0b);  // BL
+            t = mm<true, false>(n0b, Lm(0, -b));
+            t = mm<false, false>(t, Ln(a, -b));
+            mac<false, true>(w, t, m00);  // BR
+        }
+        m_axpy(q, (float)c_shapes5[k].c, w);
+        __syncthreads();  // every thread is done with `cur` before it is refilled
+    }
+    const M3<float> f = ah_quarter(q);
+    const double e = -(double)retr_mm<false, false>(f, f);
+    const int64_t s = (int64_t)t0 + tl + (int64_t)(m0 + ml) * tg.stm + (int64_t)(n0 + nl) * tg.stn + obase;
+    if (kout.p) kout.store(s, p, f);
+    if (part) {
+        const double rsum = block_sum(e, sh);
+        if (threadIdx.x == 0) part[blockIdx.x] = rsum;
+    }
+}
+
+// The tile kernel is used when the environment sets FLUE_FWD_TILE=1 (read at
+// every launch; the L1/L2 kernel is the default, see the measurements beside
+// k_fwd) for FP32 5-loop energies over spatial planes whose time extent is
+// even and whose plane extents are multiples of the patch.
+static bool fwd_tile_ok(const Geom& g, const PlaneArg& pa, int kind, bool fout, bool fits) {
+    const char* env = getenv("FLUE_FWD_TILE");
+    if (!env || atoi(env) != 1) return false;
+    if (kind != 1 || fout || !fits || g.n[0] % FT_TT) return false;
+    for (int q = 0; q < pa.np; ++q) {
+        const int mu = pa.mu[q], nu = pa.nu[q];
+        if (mu == 0 || nu == 0 || g.n[mu] % FT_TM || g.n[nu] % FT_TN) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
 // 3. line cotangents: one thread per (site, slot, length)
 // ---------------------------------------------------------------------------
 constexpr int COT_BS = FLUE_COT_BS;
 
 
-// Sum of the four corner insertions in the word that follows side q of the
-// rectangle (i0,j0,a,b):  Ka A B C + A Kb B C + A B Kc C + A B C Kd with
-// A,B,C = S_q+1, S_q+2, S_q+3 and Ka,Kb,Kc,Kd = K_q+1, K_q+2, K_q+3, K_q.
+// The other extent w and the weight of every 5-loop shape that has a side of
+// length len (shapes (len, w) and (w, len) carry the same coefficient,
+// src/wloops.F90:219-224, :327-405): row len - 1, w = 0 ends the row.
+__constant__ int c_lw_w[3][3] = {{1, 2, 3}, {2, 1, 0}, {3, 1, 0}};
+__constant__ double c_lw_c[3][3] = {{K1c, 0.5 * K3c, 0.5 * K4c}, {K2c, 0.5 * K3c, 0.0}, {K5c, 0.5 * K4c, 0.0}};
+// the same weights rounded to FP32 once (no FP64 -> FP32 conversion in the
+// FP32 kernel's inner loop)
+__constant__ float c_lw_cf[3][3] = {{(float)K1c, (float)(0.5 * K3c), (float)(0.5 * K4c)},
+                                    {(float)K2c, (float)(0.5 * K3c), 0.f},
+                                    {(float)K5c, (float)(0.5 * K4c), 0.f}};
 template <typename T>
-__device__ __forceinline__ M3<T> side_cot(const Ctx<T>& cx, const AHAoS<T>& kin, int p, int q, int i0, int j0, int a,
-                                          int b, int dagoff) {
-    const int q1 = q % 4 + 1, q2 = q1 % 4 + 1, q3 = q2 % 4 + 1;
-    // The rectangle has four distinct sites, its corners c1..c4; every side
-    // starts at one of them (S1 at c1, S2 at c2, S3 = L(c4)^+, S4 = L(c1)^+),
-    // so 4 wrapped coordinates give all 7 operand addresses.
-    const int sm0 = wrapd(cx.cm, i0, cx.nm) * (int)cx.stm, sm1 = wrapd(cx.cm, i0 + a, cx.nm) * (int)cx.stm;
-    const int sn0 = wrapd(cx.cn, j0, cx.nn) * (int)cx.stn, sn1 = wrapd(cx.cn, j0 + b, cx.nn) * (int)cx.stn;
-    const int s0 = (int)cx.s;
-    const int c1 = s0 + sm0 + sn0, c2 = s0 + sm1 + sn0, c3 = s0 + sm1 + sn1, c4 = s0 + sm0 + sn1;
-    auto corner = [&](int k) { return k == 1 ? c1 : (k == 2 ? c2 : (k == 3 ? c3 : c4)); };
-    auto side = [&](int k) {
-        const int site = (k == 2) ? c2 : (k == 3 ? c4 : c1);
-#if FLUE_LINES_DAG
-        const int plane = ((k & 1) ? cx.kmu + a - 1 : cx.knu + b - 1) + (k >= 3 ? dagoff : 0);
-        return cx.lines.load(site, plane);
-#else
-        const int plane = (k & 1) ? cx.kmu + a - 1 : cx.knu + b - 1;
-        const M3<T> m = cx.lines.load(site, plane);
-        return k >= 3 ? dag(m) : m;
-#endif
-    };
-    T kv[9];
-    const M3<T> C = side(q3);
-    M3<T> t1 = m_zero<T>();
-    kin.load_packed(corner(q), p, kv);
-    mac_xk(t1, C, kv);
-    kin.load_packed(corner(q3), p, kv);
-    mac_kx(t1, kv, C);
-    const M3<T> B = side(q2);
-    const M3<T> bc = mul(B, C);
-    M3<T> t2 = mul(B, t1);
-    kin.load_packed(corner(q2), p, kv);
-    mac_kx(t2, kv, bc);
-    const M3<T> A = side(q1);
-    const M3<T> abc = mul(A, bc);
-    M3<T> res = mul(A, t2);
-    kin.load_packed(corner(q1), p, kv);
-    mac_kx(res, kv, abc);
-    return res;
+__device__ __forceinline__ T lw_coef(int len, int k);
+template <>
+__device__ __forceinline__ float lw_coef<float>(int len, int k) {
+    return c_lw_cf[len - 1][k];
+}
+template <>
+__device__ __forceinline__ double lw_coef<double>(int len, int k) {
+    return c_lw_c[len - 1][k];
 }
 
-template <typename T>
+// Cotangent of the line l = L^len_e(P), P the thread's site, Q = P + len e.
+// In a plane (e, f) the line is a side of the rectangles of shapes with a
+// side len along e and w along f that lie on either side of it (SG = +1:
+// towards +f, -1: towards -f).  Every such side, whatever its role (S1, S2,
+// S3 = L^+, S4 = L^+), contributes the same form: going on from Q around the
+// rectangle, A = the f-line Q -> R1 = Q + SG w f, B = the e-line R1 -> R2 =
+// P + SG w f (against e, so daggered), C = the f-line R2 -> P, and
+//     dLambda = SG o coef [K(Q) A B C + A K(R1) B C + A B K(R2) C + A B C K(P)]
+// with o = +1 when e is the plane's first direction mu, -1 when it is nu
+// (the clockwise walks are the daggers of the counter-clockwise leaf words:
+// K^+ = -K).  Horner scheme, 8 products (4 with an anti-Hermitian K):
+//     K(Q) (A (B C)) + A [K(R1) (B C) + B (K(R2) C + C K(P))].
+// A is the stored line at Q (SG = +1) or the dagger of the one at R1 (-1); C
+// the dagger of the one at P (+1) or the one at R2 (-1); B the dagger of the
+// e-line at R2.  SG is a template argument, so every dagger is folded into
+// the products at compile time and only plain lines are stored.
+template <int SG, typename T, typename I>
+__device__ __forceinline__ void line_side(M3<T>& acc, T coef, const MatAoS<T>& lines, const AHAoS<T>& kin, int p,
+                                          I s, I Q, I off, int pf, int pB, const T kP[9], const T kQ[9]) {
+    constexpr bool DA = SG < 0, DC = SG > 0;
+    const I R1 = Q + off, R2 = s + off;
+    T kv[9];
+    const M3<T> C = ldm(lines, DC ? s : R2, pf);
+    M3<T> t1 = m_zero<T>();
+    mac_xk<DC>(t1, C, kP);
+    ldk(kin, R2, p, kv);
+    mac_kx<DC>(t1, kv, C);
+    const M3<T> B = ldm(lines, R2, pB);
+    const M3<T> bc = mm<true, DC>(B, C);
+    M3<T> t2 = mm<true, false>(B, t1);
+    ldk(kin, R1, p, kv);
+    mac_kx(t2, kv, bc);
+    const M3<T> A = ldm(lines, DA ? R1 : Q, pf);
+    const M3<T> abc = mm<DA, false>(A, bc);
+    M3<T> res = mm<DA, false>(A, t2);
+    mac_kx(res, kQ, abc);
+    m_axpy(acc, SG > 0 ? coef : -coef, res);
+}
+
+template <typename T, typename I>
 __global__ void __launch_bounds__(COT_BS, MinBlocks<T>::cot)
     k_linecot(Geom g, PlaneArg pa, MatAoS<T> lines, AHAoS<T> kin, MatAoS<T> lam) {
     // the 3 * nd (direction, length) tasks of one site block run in adjacent
     // blocks, so the neighbourhood they all read stays in L2
     const int ntask = 3 * pa.nd;
     const int task = blockIdx.x % ntask;
-    const int64_t s = site_block(blockIdx.x / ntask, g, blockDim.x) * blockDim.x + threadIdx.x;
-    if (s >= g.V) return;
+    const int64_t s64 = site_block(blockIdx.x / ntask, g, blockDim.x) * blockDim.x + threadIdx.x;
+    if (s64 >= g.V) return;
+    const I s = (I)s64;
     const int slot = task / 3;
     const int len = task % 3 + 1;
-    const int d = sel(pa.dir, slot);
+    const int e = sel(pa.dir, slot);
     int c[4];
-    site_coords(g, s, c);
+    site_coords(g, s64, c);
+    int ce = 0, ne = 1;
+    int64_t ste = 1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (k == e) ce = c[k], ne = g.n[k], ste = g.st[k];
+    const I Q = s + (I)((int64_t)wrapd(ce, len, ne) * ste);
+    const int pB = 3 * slot + len - 1;
+    const int nw = len == 1 ? 3 : 2;
     M3<T> acc = m_zero<T>();
     for (int p = 0; p < pa.np; ++p) {
         const int pmu = sel(pa.mu, p), pnu = sel(pa.nu, p);
-        const bool is_mu = pmu == d, is_nu = pnu == d;
-        if (!is_mu && !is_nu) continue;
-        const Ctx<T> cx = make_ctx(lines, g, s, c, pmu, pnu, sel(pa.slot, pmu), sel(pa.slot, pnu));
-        // A mu-line of length len is side S1 of the rectangle anchored at the
-        // site and S3 (daggered) of the one anchored b below, for every shape
-        // (len, b); a nu-line is S2 of the rectangle anchored a to the left
-        // and S4 (daggered) of the one anchored at the site, for every shape
-        // (a, len).  One loop, one copy of the 8-product body.
+        if (pmu != e && pnu != e) continue;
+        const int f = pmu == e ? pnu : pmu;
+        const T o = pmu == e ? T(1) : T(-1);
+        int cf = 0, nf = 1;
+        int64_t stf = 1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k == f) cf = c[k], nf = g.n[k], stf = g.st[k];
+        const int kf = 3 * sel(pa.slot, f);
+        T kP[9], kQ[9];
+        ldk(kin, s, p, kP);
+        ldk(kin, Q, p, kQ);
 #pragma unroll 1
-        for (int t = 0; t < 14; ++t) {
-            const int k = t >> 1, second = t & 1;
-            const int a = c_shapes5[k].a, b = c_shapes5[k].b;
-            if ((is_mu ? a : b) != len) continue;
-            const int q = is_mu ? (second ? 3 : 1) : (second ? 4 : 2);
-            const int i0 = (q == 2) ? -a : 0, j0 = (q == 3) ? -b : 0;
-            const M3<T> r = side_cot(cx, kin, p, q, i0, j0, a, b, 3 * pa.nd);
-            const T coef = (T)c_shapes5[k].c;
-            if (second)
-                m_axpy_dag(acc, coef, r);
-            else
-                m_axpy(acc, coef, r);
+        for (int j = 0; j < nw; ++j) {
+            const int w = c_lw_w[len - 1][j];
+            const T coef = lw_coef<T>(len, j) * o;
+            const int pf = kf + w - 1;
+            line_side<+1>(acc, coef, lines, kin, p, s, Q, (I)((int64_t)wrapd(cf, w, nf) * stf), pf, pB, kP, kQ);
+            line_side<-1>(acc, coef, lines, kin, p, s, Q, (I)((int64_t)wrapd(cf, -w, nf) * stf), pf, pB, kP, kQ);
         }
     }
-    lam.store(s, 3 * slot + len - 1, acc);
+    lam.store(s64, 3 * slot + len - 1, acc);
 }
 
 // ---------------------------------------------------------------------------
@@ -538,7 +735,7 @@ static EnergyWs energy_layout(const Geom& g, int prec, const PlaneArg& pa, bool 
     const int nbx = (int)((g.V + FWD_BS - 1) / FWD_BS);
     w.lines = 0;
     // daggered line copies only when the line cotangents run
-    w.kbuf = align256(w.lines + mat((FLUE_LINES_DAG && with_force ? 6 : 3) * pa.nd));
+    w.kbuf = align256(w.lines + mat(3 * pa.nd));
     w.lam = align256(w.kbuf + (with_force ? ah(pa.np) : 0));
     w.part = align256(w.lam + (with_force ? mat(3 * pa.nd) : 0));
     w.total = align256(w.part + (size_t)pa.np * nbx * sizeof(double));
@@ -602,11 +799,27 @@ static cudaError_t energy_fwd_part(const L& U, const Geom& g, const Geom& gs, in
     double* part = out_E ? (double*)(ws + w.part) : nullptr;
     const unsigned nbx = (unsigned)((g.V + FWD_BS - 1) / FWD_BS);
     stage_mark(0, st);
-    note_launch(), k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, gs, t0, pa, lines,
-                                                                                         with_force ? 1 : 0);
+    note_launch(), k_lines<L, T><<<dim3((unsigned)((g.V + 127) / 128), pa.nd), 128, 0, st>>>(U, g, gs, t0, pa, lines);
     stage_mark(1, st);
     const PatchArg pt = FLUE_FWD_PATCH ? make_patch(g, pa, FWD_BS) : PatchArg{};
-    note_launch(), k_fwd<T><<<nbx * pa.np, FWD_BS, 0, st>>>(g, pa, kind, pt, lines, kb, fout, part);
+    const bool fits = MatAoS<T>::fits32(g.V, 3 * pa.nd);
+    bool tiled = false;
+    if constexpr (sizeof(T) == 4) {
+        if (fwd_tile_ok(g, pa, kind, fout.p != nullptr, fits)) {
+            static_assert(FT_BS == FWD_BS, "the tile forward writes one partial per FWD_BS sites");
+            // (the attribute is per function and per device; setting it again is harmless)
+            cudaError_t ae = cudaFuncSetAttribute(k_fwd_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FT_SMEM);
+            if (ae != cudaSuccess) return ae;
+            note_launch(), k_fwd_tile<<<nbx * pa.np, FT_BS, FT_SMEM, st>>>(g, pa, lines, kb, part);
+            tiled = true;
+        }
+    }
+    if (!tiled) {
+        if (fits)
+            note_launch(), k_fwd<T, uint32_t><<<nbx * pa.np, FWD_BS, 0, st>>>(g, pa, kind, pt, lines, kb, fout, part);
+        else
+            note_launch(), k_fwd<T, int64_t><<<nbx * pa.np, FWD_BS, 0, st>>>(g, pa, kind, pt, lines, kb, fout, part);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (out_E) {
@@ -616,7 +829,10 @@ static cudaError_t energy_fwd_part(const L& U, const Geom& g, const Geom& gs, in
     stage_mark(2, st);
     if (!with_force) return cudaSuccess;
     const unsigned nbc = (unsigned)((g.V + COT_BS - 1) / COT_BS);
-    note_launch(), k_linecot<T><<<nbc * 3 * pa.nd, COT_BS, 0, st>>>(g, pa, lines, kb, lam);
+    if (MatAoS<T>::fits32(g.V, 3 * pa.nd) && AHAoS<T>::fits32(g.V, pa.np))
+        note_launch(), k_linecot<T, uint32_t><<<nbc * 3 * pa.nd, COT_BS, 0, st>>>(g, pa, lines, kb, lam);
+    else
+        note_launch(), k_linecot<T, int64_t><<<nbc * 3 * pa.nd, COT_BS, 0, st>>>(g, pa, lines, kb, lam);
     stage_mark(3, st);
     return cudaGetLastError();
 }

@@ -302,3 +302,33 @@ def test_host_buffer_misaligned_input(dt, code, src, monkeypatch):
     b2, g2 = run(mis)
     assert abs(b2 - b1) < 1e-12 * abs(b1)
     assert np.array_equal(g2, g1)
+
+
+@pytest.mark.parametrize("prec", ["c64", "r12"])
+def test_forward_tile_variant(prec, monkeypatch):
+    """The forward with the lines staged per timeslice tile in shared memory
+    (FLUE_FWD_TILE=1: 2 time slices x 8 x 8 patches, cp.async) against the
+    default forward (lines read through L1/L2) and the oracle: B^2 alone, B^2
+    and its gradient, in one pass and in time slabs; a lattice the tiles do
+    not fit falls back to the default kernel."""
+    U = generate.random_field((4, 8, 8, 16), 0.4, 21)
+    bo = oracle.magnetic(U)
+    go = oracle.loop5_energy_force(U, oracle.B2_PLANES)
+    f = GaugeField.from_array(U, prec=prec)
+    monkeypatch.setenv("FLUE_FWD_TILE", "0")
+    b0, g0 = forces.magnetic_force(f)
+    g0 = _np(g0).copy()
+    m0 = G.magnetic(f)
+    monkeypatch.setenv("FLUE_FWD_TILE", "1")
+    for slabs in ("1", "2"):
+        monkeypatch.setenv("FLUE_SLABS", slabs)
+        b1, g1 = forces.magnetic_force(f)
+        g1 = _np(g1).astype(np.complex128)
+        assert abs(b1 - b0) < 1e-6 * abs(b0)
+        assert abs(G.magnetic(f) - m0) < 1e-6 * abs(m0)
+        assert np.linalg.norm(g1 - g0) < 1e-6 * np.linalg.norm(g0)
+        assert abs(b1 - bo) < 1e-6 * abs(bo)
+        assert np.linalg.norm(g1 - go) < 1e-6 * np.linalg.norm(go)
+    U2 = generate.random_field((4, 6, 8, 8), 0.4, 22)  # NX = 6: no 8 x 8 patch in the planes with x
+    b2 = G.magnetic(GaugeField.from_array(U2, prec=prec))
+    assert abs(b2 - oracle.magnetic(U2)) < 1e-6 * abs(oracle.magnetic(U2))
