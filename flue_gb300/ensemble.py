@@ -3,11 +3,11 @@ of uneven volume in one persistent, graph-captured launch (no reference
 counterpart: the reference's ``magnetic`` app reads and measures
 configurations one at a time, app/magnetic.f90:109-140).
 
-* :class:`Ensemble` -- device work list over a list of
+* :class:`Ensemble` -- device task list over a list of
   :class:`~flue_gb300.field.GaugeField` of one precision; ``run()`` replays a
-  CUDA graph (memset of the work counter + persistent kernel + per-field
-  finisher, or in pipeline mode the per-field kernel pipelines) and returns
-  per-field observables.
+  CUDA graph (memset of the scheduler counters + one cooperative persistent
+  kernel + per-field finisher, or in pipeline mode the per-field kernel
+  pipelines) and returns per-field observables.
 * :func:`autotune` -- the project's tile tuner: times candidate (columns per
   item, block size, blocks per SM) on the actual ensemble and caches the
   winner in a JSON file keyed by GPU name and ensemble signature.
@@ -48,17 +48,19 @@ def _signature(fields: Sequence[GaugeField], with_b2: bool) -> str:
 
 
 class Ensemble:
-    """``mode="persistent"`` (default): one persistent launch over all
-    fields' work items (leaves walked link by link, no scratch).
+    """``mode="persistent"`` (default): ONE cooperative persistent launch (plus
+    a per-field finisher) over all fields: blocks take tasks from a counter --
+    the straight lines of a time slab, the line-based 5-loop F and B^2
+    partials of a chunk of the slab (waiting, bounded, only on the lines of
+    that slab), and plaquettes / Polyakov loops of a run of time columns.
     ``mode="pipeline"``: per field the device entry points (plaquettes,
-    Polyakov loop, line-based B^2 on time slabs) with one library
-    workspace of the largest field's size, all captured into one graph;
-    same outputs, several kernels per field.  The pipeline computes each
-    5-loop leaf from precomputed lines (84 products per plane-site against
-    180): on a GB300, 96 fields of 16^3x32 .. 32^3x64, 137 ms against 467 ms
-    per FP32 evaluation and 3.5 s against 8.6 s in FP64."""
+    Polyakov loop, line-based B^2 on time slabs) with one library workspace
+    of the largest field's size, all captured into one graph; same outputs,
+    several kernels per field.  Both modes replay from a CUDA graph.  A
+    scheduler wait that runs out (which does not happen in a healthy run)
+    makes the outputs NaN and ``run`` raise."""
 
-    def __init__(self, fields: Sequence[GaugeField], tile=None, block=256, blocks_per_sm=2, with_b2=True,
+    def __init__(self, fields: Sequence[GaugeField], tile=None, block=128, blocks_per_sm=3, with_b2=True,
                  tune=False, mode="persistent"):
         if not fields:
             raise ValueError("empty ensemble")
@@ -76,7 +78,11 @@ class Ensemble:
         elif tune:
             tile, block, blocks_per_sm = autotune(self.fields, with_b2=self.with_b2)
         elif tile is None:
-            tile = 4
+            # measured on GB300, 96 fields of 16^3x32 .. 32^3x64: 16 columns per
+            # plaquette / Polyakov task, 128 threads, 3 blocks per SM: 111 ms
+            # FP32 (c64) and 3.46 s FP64 per evaluation (pipeline mode 115 ms,
+            # 3.48 s); 4 columns 118 ms, 2 blocks per SM 146 ms
+            tile = 16
         self.config = (int(tile), int(block), int(blocks_per_sm))
         self._descs = (_lib.FlueField * len(fields))(*[f.descriptor() for f in fields])
         self._h = ctypes.c_void_p()
@@ -107,7 +113,11 @@ class Ensemble:
 
     def run(self, graph=True) -> np.ndarray:
         self.launch(graph)
-        return self.out.cpu().numpy()
+        raw = self.out.cpu().numpy()
+        if np.isnan(raw).any():
+            raise _lib.FlueError("flue_ensemble_run", _lib.FLUE_ERR_TIMEOUT,
+                                 "a wait of the persistent scheduler ran out; outputs are NaN")
+        return raw
 
     def observables(self, graph=True) -> List[Dict[str, float]]:
         """Per field: mean plaquettes <Re Tr P>/3 (total, spatial, temporal),
