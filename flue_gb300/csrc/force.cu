@@ -402,33 +402,37 @@ __device__ __forceinline__ double lw_coef<double>(int len, int k) {
 //     dLambda = SG o coef [K(Q) A B C + A K(R1) B C + A B K(R2) C + A B C K(P)]
 // with o = +1 when e is the plane's first direction mu, -1 when it is nu
 // (the clockwise walks are the daggers of the counter-clockwise leaf words:
-// K^+ = -K).  Horner scheme, 8 products (4 with an anti-Hermitian K):
-//     K(Q) (A (B C)) + A [K(R1) (B C) + B (K(R2) C + C K(P))].
-// A is the stored line at Q (SG = +1) or the dagger of the one at R1 (-1); C
-// the dagger of the one at P (+1) or the one at R2 (-1); B the dagger of the
-// e-line at R2.  SG is a template argument, so every dagger is folded into
-// the products at compile time and only plain lines are stored.
+// K^+ = -K).  K(Q) and K(P) are the same for every rectangle of the plane,
+// so their two terms are summed over the plane's rectangles first:
+//     Lambda_plane = K(Q) X + X K(P) + sum_sides SG o coef A Y,
+//     X = sum_sides SG o coef A B C,   Y = K(R1) (B C) + B (K(R2) C),
+// 4 full products and 2 with an anti-Hermitian K per side, and 2 of the
+// latter per plane.  A is the stored line at Q (SG = +1) or the dagger of
+// the one at R1 (-1); C the dagger of the one at P (+1) or the one at R2
+// (-1); B the dagger of the e-line at R2.  SG is a template argument, so
+// every dagger is folded into the products at compile time and only plain
+// lines are stored.
 template <int SG, typename T, typename I>
-__device__ __forceinline__ void line_side(M3<T>& acc, T coef, const MatAoS<T>& lines, const AHAoS<T>& kin, int p,
-                                          I s, I Q, I off, int pf, int pB, const T kP[9], const T kQ[9]) {
+__device__ __forceinline__ void line_side(M3<T>& acc, M3<T>& X, T coef, const MatAoS<T>& lines, const AHAoS<T>& kin,
+                                          int p, I s, I Q, I off, int pf, int pB) {
     constexpr bool DA = SG < 0, DC = SG > 0;
     const I R1 = Q + off, R2 = s + off;
     T kv[9];
     const M3<T> C = ldm(lines, DC ? s : R2, pf);
-    M3<T> t1 = m_zero<T>();
-    mac_xk<DC>(t1, C, kP);
+    M3<T> t = m_zero<T>();
     ldk(kin, R2, p, kv);
-    mac_kx<DC>(t1, kv, C);
+    mac_kx<DC>(t, kv, C);
     const M3<T> B = ldm(lines, R2, pB);
+    M3<T> y = mm<true, false>(B, t);
     const M3<T> bc = mm<true, DC>(B, C);
-    M3<T> t2 = mm<true, false>(B, t1);
     ldk(kin, R1, p, kv);
-    mac_kx(t2, kv, bc);
+    mac_kx(y, kv, bc);
     const M3<T> A = ldm(lines, DA ? R1 : Q, pf);
     const M3<T> abc = mm<DA, false>(A, bc);
-    M3<T> res = mm<DA, false>(A, t2);
-    mac_kx(res, kQ, abc);
-    m_axpy(acc, SG > 0 ? coef : -coef, res);
+    const M3<T> ay = mm<DA, false>(A, y);
+    const T sc = SG > 0 ? coef : -coef;
+    m_axpy(X, sc, abc);
+    m_axpy(acc, sc, ay);
 }
 
 template <typename T, typename I>
@@ -466,17 +470,20 @@ __global__ void __launch_bounds__(COT_BS, MinBlocks<T>::cot)
         for (int k = 0; k < 4; ++k)
             if (k == f) cf = c[k], nf = g.n[k], stf = g.st[k];
         const int kf = 3 * sel(pa.slot, f);
-        T kP[9], kQ[9];
-        ldk(kin, s, p, kP);
-        ldk(kin, Q, p, kQ);
+        M3<T> X = m_zero<T>();
 #pragma unroll 1
         for (int j = 0; j < nw; ++j) {
             const int w = c_lw_w[len - 1][j];
             const T coef = lw_coef<T>(len, j) * o;
             const int pf = kf + w - 1;
-            line_side<+1>(acc, coef, lines, kin, p, s, Q, (I)((int64_t)wrapd(cf, w, nf) * stf), pf, pB, kP, kQ);
-            line_side<-1>(acc, coef, lines, kin, p, s, Q, (I)((int64_t)wrapd(cf, -w, nf) * stf), pf, pB, kP, kQ);
+            line_side<+1>(acc, X, coef, lines, kin, p, s, Q, (I)((int64_t)wrapd(cf, w, nf) * stf), pf, pB);
+            line_side<-1>(acc, X, coef, lines, kin, p, s, Q, (I)((int64_t)wrapd(cf, -w, nf) * stf), pf, pB);
         }
+        T kv[9];
+        ldk(kin, Q, p, kv);
+        mac_kx(acc, kv, X);
+        ldk(kin, s, p, kv);
+        mac_xk(acc, X, kv);
     }
     lam.store(s64, 3 * slot + len - 1, acc);
 }
