@@ -371,26 +371,6 @@ static bool fwd_tile_ok(const Geom& g, const PlaneArg& pa, int kind, bool fout, 
 constexpr int COT_BS = FLUE_COT_BS;
 
 
-// The other extent w and the weight of every 5-loop shape that has a side of
-// length len (shapes (len, w) and (w, len) carry the same coefficient,
-// src/wloops.F90:219-224, :327-405): row len - 1, w = 0 ends the row.
-__constant__ int c_lw_w[3][3] = {{1, 2, 3}, {2, 1, 0}, {3, 1, 0}};
-__constant__ double c_lw_c[3][3] = {{K1c, 0.5 * K3c, 0.5 * K4c}, {K2c, 0.5 * K3c, 0.0}, {K5c, 0.5 * K4c, 0.0}};
-// the same weights rounded to FP32 once (no FP64 -> FP32 conversion in the
-// FP32 kernel's inner loop)
-__constant__ float c_lw_cf[3][3] = {{(float)K1c, (float)(0.5 * K3c), (float)(0.5 * K4c)},
-                                    {(float)K2c, (float)(0.5 * K3c), 0.f},
-                                    {(float)K5c, (float)(0.5 * K4c), 0.f}};
-template <typename T>
-__device__ __forceinline__ T lw_coef(int len, int k);
-template <>
-__device__ __forceinline__ float lw_coef<float>(int len, int k) {
-    return c_lw_cf[len - 1][k];
-}
-template <>
-__device__ __forceinline__ double lw_coef<double>(int len, int k) {
-    return c_lw_c[len - 1][k];
-}
 
 // Cotangent of the line l = L^len_e(P), P the thread's site, Q = P + len e.
 // In a plane (e, f) the line is a side of the rectangles of shapes with a
