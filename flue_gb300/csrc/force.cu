@@ -218,6 +218,10 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -291,10 +295,12 @@ __global__ void __launch_bounds__(FT_BS, 2)
             cn += cn < 0 ? tg.nn : 0;
             cn -= cn >= tg.nn ? tg.nn : 0;
             const uint32_t site = (uint32_t)(t0 + tt + cm * tg.stm + cn * tg.stn + obase);
-            const float4* src = lines.unit0_32(site, isn ? knu + b - 1 : kmu + a - 1);
+            const int plane = isn ? knu + b - 1 : kmu + a - 1;
+            const float4* src = lines.unit0_32(site, plane);
             float4* dst = buf + pos * 5;
 #pragma unroll
-            for (int u = 0; u < 5; ++u) cp_async16(dst + u, src + 32 * u);
+            for (int u = 0; u < 4; ++u) cp_async16(dst + u, src + 32 * u);
+            cp_async8(dst + 4, lines.unit4_32(site, plane));
         }
         cp_async_commit();
     };
