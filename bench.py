@@ -201,7 +201,7 @@ def bench_config(args, dims, n_replicas):
     return {"workload": f"5-loop F_munu + B^2 forward + backward (su(3) gradient), {nx}^3x{nt}",
             "lattice": [nt, nx, ny, nz], "sites": nt * nx * ny * nz, "field_format": args.prec, "eps": args.eps,
             "seed": args.seed, "global_batch": n_replicas, "parallelism": f"replicas x{n_replicas}",
-            "l2": "inputs and intermediates larger than L2 (field 0.4-0.6 GB, 12 GB DRAM traffic per step)"}
+            "l2": "inputs and intermediates larger than L2 (field 0.4-0.6 GB, 8 GB DRAM traffic per step)"}
 
 
 def ensemble_bench(steps: int):
@@ -220,7 +220,7 @@ def ensemble_bench(steps: int):
     torch.cuda.synchronize()
     gen_s = time.perf_counter() - t0
     out = {"fields": len(dims), "sites": sites, "gen_s": gen_s}
-    cands = [(t, b, m) for t in (2, 8, 32) for b in (128, 256) for m in (1, 4)]
+    cands = [(t, b, m) for t in (4, 16, 32) for b in (128, 256) for m in (1, 3)]
     cfg = E.autotune(f32, candidates=cands, reps=1)
     b2s = {}
     from flue_gb300 import _lib
@@ -428,7 +428,7 @@ def run_reference(args, dims, ws, rank):
 
 # DRAM bytes (read + write) per site of one device step, from the ncu capture of this bench
 # (profiles/dram_traffic_b2_step_32x64.md: 16 time slabs at 32^3x64, reconstruct-12).
-TRAFFIC_PER_SITE = {("r12", (64, 32, 32, 32)): 5898.0}
+TRAFFIC_PER_SITE = {("r12", (64, 32, 32, 32)): 3886.5}
 
 
 def step_traffic(prec, dims):
