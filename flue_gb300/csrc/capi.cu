@@ -759,7 +759,7 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
         if (!d_grad) continue;
         if ((e = cudaStreamWaitEvent(c->s_out, c->ev_cp[j], 0)) != cudaSuccess) break;
         const unsigned ob = k == nslab - 1 ? 0u : out_blocks;
-        if ((e = launch_energy_slab_out(U, 0, n, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, ob, c->s_out,
+        if ((e = launch_energy_slab_out(U, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, ob, c->s_out,
                                         data_dtype)) != cudaSuccess)
             break;
         if ((e = cudaEventRecord(c->ev_out[j], c->s_out)) != cudaSuccess) break;

@@ -93,17 +93,16 @@ cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, 
 // normalised by vfull, line cotangents when with_force) computes the slab of
 // time slices [t0, t0 + nts) of field U (the whole field, or a packed slab
 // with t0 = 0).  Part 2 (link cotangents into the full-lattice gradient of
-// time extent ntf at time offset t0, grid capped at max_blocks per direction
-// when > 0) takes the slab as time slices [lt0, lt0 + nts) of field U (the
-// link cotangents read the links themselves) and writes the gradient as
+// time extent ntf, grid capped at max_blocks per direction when > 0) takes U
+// with the slab's geometry (links unused) and writes the gradient as
 // out_dtype: the compute dtype, or complex128 (PREC_C128) from an FP32
 // computation.  Both use the same workspace, sized for the slab, and may run
 // on different streams.
 cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const PlaneSet& ps, int64_t vfull,
                                    double* out_E, bool with_force, void* ws, size_t ws_bytes, cudaStream_t st);
-cudaError_t launch_energy_slab_out(const FieldRef& U, int lt0, int nts, const PlaneSet& ps, int64_t vfull, int ntf,
-                                   int t0, void* force, int force_form, void* ws, size_t ws_bytes, unsigned max_blocks,
-                                   cudaStream_t st, int out_dtype);
+cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
+                                   int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st,
+                                   int out_dtype);
 // launch_energy over nslab time slabs on nstream (<= 4) streams forked from
 // st (plane sets without the time direction); workspace of
 // energy_slabs_ws_bytes(...) bytes.  Results equal launch_energy's: the

@@ -477,15 +477,10 @@ __global__ void __launch_bounds__(COT_BS, MinBlocks<T>::cot)
 // ---------------------------------------------------------------------------
 // 4. link cotangents and gradient output: one thread per (site, direction),
 //    grid-strided so that a capped grid can write the gradient to host memory
-//    beside other kernels.  The 1-link "lines" U are read from the field
-//    itself (48 bytes per link in reconstruct-12 against 72 for the stored
-//    line; the sites of geometry g are time slices [lt0, lt0 + g.n[0]) of a
-//    field of geometry gs), the 2-link lines and the line cotangents from the
-//    workspace.
+//    beside other kernels
 // ---------------------------------------------------------------------------
-template <class L, typename T>
-__global__ void k_linkcot(L U, Geom g, Geom gs, int lt0, PlaneArg pa, MatAoS<T> lines, MatAoS<T> lam, T scale,
-                          int form, RefOut<T> out) {
+template <typename T>
+__global__ void k_linkcot(Geom g, PlaneArg pa, MatAoS<T> lines, MatAoS<T> lam, T scale, int form, RefOut<T> out) {
     const int d = blockIdx.y;
     const int slot = sel(pa.slot, d);
     for (int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; z < g.V; z += (int64_t)gridDim.x * blockDim.x) {
@@ -496,18 +491,15 @@ __global__ void k_linkcot(L U, Geom g, Geom gs, int lt0, PlaneArg pa, MatAoS<T> 
         int c[4];
         site_coords(g, z, c);
         int cd = 0, nd = 1;
-        int64_t sd = 1, su = 1;
+        int64_t sd = 1;
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-            if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k], su = gs.st[k];
-        const int wp = wrapd(cd, 1, nd), wm = wrapd(cd, -1, nd);
-        const int64_t zp = z + (int64_t)wp * sd, zm = z + (int64_t)wm * sd,
+            if (k == d) cd = c[k], nd = g.n[k], sd = g.st[k];
+        const int64_t zp = z + (int64_t)wrapd(cd, 1, nd) * sd, zm = z + (int64_t)wrapd(cd, -1, nd) * sd,
                       zmm = z + (int64_t)wrapd(cd, -2, nd) * sd;
-        // the link of site z in the field, and its neighbours along d
-        const int64_t u = (int64_t)(lt0 + c[0]) + c[1] * gs.st[1] + c[2] * gs.st[2] + c[3] * gs.st[3];
-        const int l2 = 3 * slot + 1;
-        const M3<T> up = U.load(u + (int64_t)wp * su, d);
-        const M3<T> um = U.load(u + (int64_t)wm * su, d);
+        const int l1 = 3 * slot, l2 = 3 * slot + 1;
+        const M3<T> up = lines.load(zp, l1);
+        const M3<T> um = lines.load(zm, l1);
         M3<T> n = lam.load(z, 3 * slot);
         mac<false, false>(n, up, lam.load(z, 3 * slot + 1));
         mac<false, false>(n, lam.load(zm, 3 * slot + 1), um);
@@ -518,7 +510,7 @@ __global__ void k_linkcot(L U, Geom g, Geom gs, int lt0, PlaneArg pa, MatAoS<T> 
         }
         mac<false, false>(n, lam.load(zmm, 3 * slot + 2), lines.load(zmm, l2));
         if (form == 0) {
-            const M3<T> un = mul(U.load(u, d), n);
+            const M3<T> un = mul(lines.load(z, l1), n);
             out.store(z, d, ta_scaled(un, T(-0.5) * scale));
         } else {
             out.store(z, d, m_scale(dag(n), scale));
@@ -663,19 +655,16 @@ static cudaError_t energy_fwd_part(const L& U, const Geom& g, const Geom& gs, in
     return cudaGetLastError();
 }
 
-// Part 2: link cotangents, gradient of E/vnorm written through `fo`; the
-// sites of g are time slices [lt0, lt0 + g.n[0]) of the field U of
-// geometry gs.
-template <class L, typename T>
-static cudaError_t energy_out_part(const L& U, const Geom& g, const Geom& gs, int lt0, const PlaneArg& pa,
-                                   double vnorm, int form, char* ws, const EnergyWs& w, RefOut<T> fo,
-                                   unsigned max_blocks, cudaStream_t st) {
+// Part 2: link cotangents, gradient of E/vnorm written through `fo`.
+template <typename T>
+static cudaError_t energy_out_part(const Geom& g, const PlaneArg& pa, double vnorm, int form, char* ws,
+                                   const EnergyWs& w, RefOut<T> fo, unsigned max_blocks, cudaStream_t st) {
     MatAoS<T> lines{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lines), g.V};
     MatAoS<T> lam{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lam), g.V};
     const T scale = (T)(-1.0 / (2.0 * vnorm));
     unsigned nb = (unsigned)((g.V + 127) / 128);
     if (max_blocks && nb > max_blocks) nb = max_blocks;
-    note_launch(), k_linkcot<L, T><<<dim3(nb, 4), 128, 0, st>>>(U, g, gs, lt0, pa, lines, lam, scale, form, fo);
+    note_launch(), k_linkcot<T><<<dim3(nb, 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo);
     stage_mark(4, st);
     return cudaGetLastError();
 }
@@ -688,7 +677,7 @@ static cudaError_t energy_impl(const L& U, const Geom& g, const PlaneArg& pa, in
         energy_fwd_part<L, T>(U, g, g, 0, pa, kind, out_E, force != nullptr, (double)g.V, ws, w, fout, st);
     if (e != cudaSuccess || !force) return e;
     RefOut<T> fo{(C2*)force, g.V, 4};
-    return energy_out_part<L, T>(U, g, g, 0, pa, (double)g.V, form, ws, w, fo, 0, st);
+    return energy_out_part<T>(g, pa, (double)g.V, form, ws, w, fo, 0, st);
 }
 
 cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, void* force, int force_form, void* ws,
@@ -725,25 +714,21 @@ cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const Pla
     return cudaSuccess;
 }
 
-cudaError_t launch_energy_slab_out(const FieldRef& U, int lt0, int nts, const PlaneSet& ps, int64_t vfull, int ntf,
-                                   int t0, void* force, int force_form, void* ws, size_t ws_bytes, unsigned max_blocks,
-                                   cudaStream_t st, int out_dtype) {
-    if (has_time_plane(ps) || lt0 < 0 || nts < 1 || lt0 + nts > U.g.n[0] || t0 < 0 || t0 + nts > ntf)
-        return cudaErrorInvalidValue;
-    const Geom g = make_geom(nts, U.g.n[1], U.g.n[2], U.g.n[3]);
-    if (vfull < g.V) return cudaErrorInvalidValue;
+cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
+                                   int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st,
+                                   int out_dtype) {
+    if (has_time_plane(ps) || vfull < U.g.V || t0 < 0 || t0 + U.g.n[0] > ntf) return cudaErrorInvalidValue;
     const PlaneArg pa = make_planes(ps);
-    const EnergyWs w = energy_layout(g, U.prec, pa, true);
+    const EnergyWs w = energy_layout(U.g, U.prec, pa, true);
     if (ws_bytes < w.total) return cudaErrorInvalidValue;
-    if (U.prec == PREC_C128 && out_dtype != PREC_C128) return cudaErrorInvalidValue;
-    FLUE_DISPATCH_LINKS(U, {
-        using C2 = typename V2<T>::type;
-        RefOut<T> fo{(C2*)force, vfull, 4, nts, ntf, t0};
-        if (sizeof(T) == 4 && out_dtype == PREC_C128) fo.p = nullptr, fo.pd = (double2*)force;
-        return energy_out_part<decltype(L), T>(L, g, U.g, lt0, pa, (double)vfull, force_form, (char*)ws, w, fo,
-                                               max_blocks, st);
-    });
-    return cudaSuccess;
+    if (U.prec == PREC_C128) {
+        if (out_dtype != PREC_C128) return cudaErrorInvalidValue;
+        RefOut<double> fo{(double2*)force, vfull, 4, U.g.n[0], ntf, t0};
+        return energy_out_part<double>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
+    }
+    RefOut<float> fo{(float2*)force, vfull, 4, U.g.n[0], ntf, t0};
+    if (out_dtype == PREC_C128) fo.p = nullptr, fo.pd = (double2*)force;
+    return energy_out_part<float>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -833,7 +818,8 @@ cudaError_t launch_energy_slabs(const FieldRef& U, const PlaneSet& ps, double* o
         char* slot = (char*)ws + (size_t)i * w.slot;
         e = launch_energy_slab_fwd(U, t0, n, ps, U.g.V, spart ? spart + k : nullptr, with_force, slot, w.slot, sk);
         if (e == cudaSuccess && with_force) {
-            e = launch_energy_slab_out(U, t0, n, ps, U.g.V, U.g.n[0], t0, force, form, slot, w.slot, 0, sk,
+            const FieldRef Us{U.links, make_geom(n, U.g.n[1], U.g.n[2], U.g.n[3]), U.prec};
+            e = launch_energy_slab_out(Us, ps, U.g.V, U.g.n[0], t0, force, form, slot, w.slot, 0, sk,
                                        U.prec == PREC_C128 ? PREC_C128 : PREC_C64);
         }
     }
