@@ -223,14 +223,20 @@ int flue_gluon_propagator(const flue_field *U, double xi, int mu_start, double *
  * magnetic app loops over configurations one by one, app/magnetic.f90:109-140)
  *
  * Plaquettes, Polyakov loop and B^2 of up to thousands of device fields of
- * uneven volume (all of one precision) in ONE persistent launch: each field
- * is cut into items of tile_cols time columns, a grid of blocks_per_sm x SM
- * blocks of `block` threads (128 or 256) takes items from an atomic counter
- * (no block waits on another), a finisher sums each field's items in order.
+ * uneven volume (all of one precision) in ONE persistent launch.  The launch
+ * is cooperative (every block resident; a grid of blocks_per_sm x SM blocks
+ * of `block` threads, 128 or 256, reduced to what fits) and works through a
+ * task list from an atomic counter: the 5-loop lines of a chunk of a time
+ * slab, the line-based B^2 of a chunk (each waiting, with a bounded wait,
+ * for its slab's lines), and plaquettes / Polyakov loops of tile_cols time
+ * columns; a finisher sums each field's partials in list order.  A wait that
+ * runs out (not met in a healthy run) makes every output NaN.
  * Per field the output holds 6 doubles: sum Re Tr P over spatial planes, over
  * temporal planes, sum Re Tr and Im Tr of the Polyakov loop, B^2 (divided by
- * V; 0 when with_b2 = 0), V.  create() allocates the work list and partials
- * on the current device (library-owned); capture() records memset + kernel +
+ * V; 0 when with_b2 = 0), V.  create() allocates the task list, partials and
+ * a ring of four slab-line buffers on the current device (library-owned;
+ * FLUE_ENS_SLAB_SITES, read here, sets the sites per slab, default 2^17);
+ * items() returns the number of tasks; capture() records memset + kernel +
  * finisher writing to d_out into a CUDA graph, replay() launches it.
  * tile_cols = 0 selects pipeline mode instead (block, blocks_per_sm unused):
  * per field the device entry points -- flue_plaquette (spatial, temporal),
