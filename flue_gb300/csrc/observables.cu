@@ -79,11 +79,19 @@ __device__ __forceinline__ void pack_one(const SRC* __restrict__ src, const Stri
     site_coords(g, s, c);
     const int64_t base = c[0] * sd.s[0] + c[1] * sd.s[1] + c[2] * sd.s[2] + c[3] * sd.s[3] + mu * sd.s[4];
     double r[3][3], im[3][3];
+    // reconstruct-12 keeps the first two rows: without reunitarisation the
+    // third row is not read at all (in the reference's layout its elements
+    // are planes of their own, a third of the field's bytes -- a host field
+    // read over NVLink-C2C moves 2/3 of its size)
+    const int na = (dst_prec == PREC_R12 && !reun) ? 2 : 3;
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
-            const SRC v = src[base + a * sd.s[5] + b * sd.s[6]];
-            r[a][b] = (double)v.x;
-            im[a][b] = (double)v.y;
+            r[a][b] = im[a][b] = 0.0;
+            if (a < na) {
+                const SRC v = src[base + a * sd.s[5] + b * sd.s[6]];
+                r[a][b] = (double)v.x;
+                im[a][b] = (double)v.y;
+            }
         }
     if (reun) fix_su3_rows(r, im);
     if (dst_prec == PREC_C128) {

@@ -230,7 +230,9 @@ int flue_gluon_propagator(const flue_field *U, double xi, int mu_start, double *
  * slab, the line-based B^2 of a chunk (each waiting, with a bounded wait,
  * for its slab's lines), and plaquettes / Polyakov loops of tile_cols time
  * columns; a finisher sums each field's partials in list order.  A wait that
- * runs out (not met in a healthy run) makes every output NaN.
+ * runs out (not met in a healthy run) makes every output NaN.  One
+ * ensemble's evaluations share its counters and line buffers: they must not
+ * overlap on the GPU (run them in order on one stream).
  * Per field the output holds 6 doubles: sum Re Tr P over spatial planes, over
  * temporal planes, sum Re Tr and Im Tr of the Polyakov loop, B^2 (divided by
  * V; 0 when with_b2 = 0), V.  create() allocates the task list, partials and
