@@ -484,6 +484,16 @@ struct DevCache {
                 ev_end[kPipeComp - 1] = {};
     void* slot[kPipeSlots] = {};
     size_t slot_bytes[kPipeSlots] = {};
+    // copy-engine transfers of pinned host buffers: chunks of time slices
+    // copied in by 2-D DMA on s_dma into `stage` and out of the two chunk
+    // buffers `ostage` on s_dout, one event per chunk
+    static constexpr int kMaxChunks = 64;
+    cudaStream_t s_dma = nullptr, s_dout = nullptr;
+    cudaEvent_t ev_dma[kMaxChunks] = {}, ev_dout[kMaxChunks] = {};
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    void* ostage = nullptr;
+    size_t ostage_bytes = 0;
 };
 
 // A device-usable address of host memory `p`, or NULL: pinned (page-locked,
@@ -507,6 +517,21 @@ static const void* device_view(const void* p) {
         return nullptr;
     }
     return ats ? p : nullptr;
+}
+
+// Pinned (page-locked) host memory that the host-buffer force moves by
+// copy-engine copies: only when the environment variable `env_name`
+// (FLUE_DMA_IN for the field, FLUE_DMA_OUT for the gradient) is set to a
+// non-zero value; otherwise kernels read / write it.
+static bool pinned_host(const void* p, const char* env_name) {
+    const char* env = getenv(env_name);
+    if (!env || atoi(env) == 0) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
 }
 
 // Copy `bytes` between host and device on the cache's stream, as one copy or
@@ -646,6 +671,12 @@ int pipe_setup(DevCache* c) {
         e = cudaStreamCreateWithFlags(&c->s_cp[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_end[i], cudaEventDisableTiming);
     }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->s_dma, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->s_dout, cudaStreamNonBlocking);
+    for (int q = 0; q < DevCache::kMaxChunks && e == cudaSuccess; ++q) {
+        e = cudaEventCreateWithFlags(&c->ev_dma[q], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_dout[q], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) return cuda_status(e);
     c->pipe_init = true;
     return FLUE_OK;
@@ -675,14 +706,45 @@ int pipe_slabs(int NT, int64_t V) {
     return s < 1 ? 1 : s;
 }
 
-int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int NT, int NX, int NY, int NZ, int prec,
-                             int form, double* B, void* d_grad, int nslab) {
+int magnetic_force_pipelined(DevCache* c, const void* d_in, const void* h_in, void* h_grad, int data_dtype, int NT,
+                             int NX, int NY, int NZ, int prec, int form, double* B, void* d_grad, int nslab) {
     int rc = pipe_setup(c);
     if (rc) return rc;
     const int64_t V = (int64_t)NT * NX * NY * NZ;
+    const int64_t V3 = V / NT;
     const int64_t st[7] = {1, NT, (int64_t)NT * NX, (int64_t)NT * NX * NY, V, 4 * V, 12 * V};
     const int nts = (NT + nslab - 1) / nslab;
     nslab = (NT + nts - 1) / nts;
+    const size_t esz = data_dtype == FLUE_C128 ? 16 : 8;
+    // Copy-engine transfers of pinned host buffers (h_in: the field, h_grad:
+    // the gradient; opt-in, FLUE_DMA_IN / FLUE_DMA_OUT = 1).  Kernels that
+    // read or write host memory hold SMs while they wait on the host link and
+    // share one budget of it (measured on GB300 at 64x32^3 complex128:
+    // reading the field's stored rows 3.8 ms, writing the gradient 6.2 ms,
+    // both at once 10.1 ms; in the pipeline the gradient writes, 0.63 ms per
+    // slab, set the pace), while the copy engines use no SMs and move both
+    // directions at once (1.2 GB each way in 7.1 ms).  A 2-D copy moves rows
+    // of CH time slices of every (column, direction, matrix element) between
+    // the host array and a chunk buffer: 256-byte rows ran at 185 GB/s,
+    // 128-byte at 107, 64-byte at 56.  The first chunk's slabs read the field
+    // with kernels, and the copies of the other chunks start after them
+    // (copies that start at once take the host link from those reads and
+    // delay every compute); the last FLUE_OUT_TAIL slabs write their gradient
+    // with kernels.  Reconstruct-12 stages the first two matrix rows only.
+    // Measured per call at 64x32^3, 16 slabs of 4 slices, r12, 60 calls
+    // (kernel reads and writes -> copies): complex128 median 11.24 -> 10.39 ms
+    // with 16-slice chunks and no kernel-written tail (8-slice chunks 12.5,
+    // 32-slice 12.1-13.2), complex64 9.43 -> 9.20 ms with a tail of 2; but
+    // one call in 15-60 has a single copy stall for 6-27 ms (with or without
+    // other transfers beside it, whole or split into pieces of 16384 or 4096
+    // rows), against a spread of 10.9-11.6 ms with kernel transfers -- so the
+    // copies stay opt-in.
+    const int ch_env = env_int("FLUE_DMA_CHUNK", 16);  // slices per chunk, rounded up to whole slabs
+    int CH = nts * (int)(((ch_env > 0 ? ch_env : 16) + nts - 1) / nts);
+    if (CH > NT) CH = NT;
+    const int nchunk = (NT + CH - 1) / CH;
+    if (nchunk < 2 || nchunk > DevCache::kMaxChunks) h_in = h_grad = nullptr;
+    if (!d_grad) h_grad = nullptr;
     // Slab schedule.  Each slab reads, per site column, a run of n time
     // slices (n * esz bytes) from host memory; runs that straddle 64-byte
     // boundaries cost extra transfers over the host link (measured: a numpy
@@ -691,16 +753,16 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
     // starts on an A-byte boundary stays inside one 64-byte block, so when
     // the field's address is off an A-byte boundary by a whole number of
     // elements, a short first slab shifts the grid so that every later
-    // slab's runs start on one.
-    const size_t esz0 = data_dtype == FLUE_C128 ? 16 : 8;
+    // slab's runs start on one (not with copy-engine chunks, whose slabs
+    // start on multiples of the slab length).
     size_t A = 64;
-    while (A > esz0 && A > (size_t)nts * esz0) A >>= 1;
+    while (A > esz && A > (size_t)nts * esz) A >>= 1;
     int t0s[34], ns[34];
     int nsl = 0;
     {
         const size_t off = (size_t)((uintptr_t)d_in % A);
-        int first = (off && off % esz0 == 0) ? (int)((A - off) / esz0) : 0;
-        if (first >= nts || first >= NT || nslab >= 33) first = 0;
+        int first = (off && off % esz == 0) ? (int)((A - off) / esz) : 0;
+        if (first >= nts || first >= NT || nslab >= 33 || h_in || h_grad) first = 0;
         int t = 0;
         if (first) t0s[nsl] = 0, ns[nsl++] = first, t = first;
         while (t < NT) {
@@ -709,6 +771,19 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
         }
     }
     nslab = nsl;
+    // input staging: chunk q >= 1, plane (a, b) with a < R, direction mu,
+    // column, slice in the chunk
+    const int R = prec == FLUE_R12 ? 2 : 3;
+    const int64_t P = 4 * V3 * (int64_t)CH;  // elements per plane and chunk
+    if (h_in && (rc = grow(&c->stage, &c->stage_bytes, (size_t)(nchunk - 1) * R * 3 * P * esz))) return rc;
+    const int64_t sst[7] = {1, CH, (int64_t)CH * NX, (int64_t)CH * NX * NY, (int64_t)CH * V3, P, (int64_t)R * P};
+    // output staging: two chunk buffers holding a gradient of time extent CH
+    // (slices [0, Tdma) leave by copies, the tail by kernel writes)
+    int ztail = env_int("FLUE_OUT_TAIL", esz == 16 ? 0 : 2);
+    ztail = ztail < 0 ? 0 : ztail;
+    const int Tdma = !h_grad ? 0 : (ztail == 0 ? NT : (nslab > ztail ? t0s[nslab - ztail] : 0));
+    const size_t Bo = (size_t)(9 * P) * esz;
+    if (Tdma && (rc = grow(&c->ostage, &c->ostage_bytes, 2 * Bo))) return rc;
     const PlaneSet ps = b2_planes();
     const Geom g0 = make_geom(nts, NX, NY, NZ);
     const size_t fbytes = ((size_t)flue_field_bytes(nts, NX, NY, NZ, prec) + 255) & ~(size_t)255;
@@ -731,11 +806,16 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
     // run on the whole GPU (8 slabs: 11.95 -> 11.79 ms per call).
     const unsigned in_blocks = (unsigned)env_int("FLUE_IN_BLOCKS", 32);
     const unsigned out_blocks = (unsigned)env_int("FLUE_OUT_BLOCKS", 16);
-    const size_t esz = data_dtype == FLUE_C128 ? 16 : 8;
     cudaError_t e = cudaEventRecord(c->ev_go, c->st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_in, c->ev_go, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_out, c->ev_go, 0);
+    if (e == cudaSuccess && Tdma) e = cudaStreamWaitEvent(c->s_dout, c->ev_go, 0);
     for (int i = 1; i < ncomp && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(c->s_cp[i - 1], c->ev_go, 0);
+    // the slab after whose read the field's copies start (FLUE_DMA_AFTER,
+    // default the first chunk's last slab)
+    int kdma = env_int("FLUE_DMA_AFTER", CH / nts - 1);
+    kdma = kdma < 0 ? 0 : (kdma > CH / nts - 1 ? CH / nts - 1 : kdma);
+    int last_dout = -1;
     for (int k = 0; k < nslab && e == cudaSuccess; ++k) {
         const int j = k % nslot, t0 = t0s[k], n = ns[k];
         cudaStream_t cs = (k % ncomp) == 0 ? c->st : c->s_cp[k % ncomp - 1];
@@ -744,10 +824,35 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
         const FieldRef U{buf, g, prec};
         // pack slab k once the compute of slab k - nslot has read this slot
         if (k >= nslot && (e = cudaStreamWaitEvent(c->s_in, c->ev_cp[j], 0)) != cudaSuccess) break;
-        if ((e = launch_pack((const char*)d_in + (size_t)t0 * esz, data_dtype, st, g, buf, prec, 0, c->s_in,
-                             k == 0 ? 0u : in_blocks)) != cudaSuccess)
+        if (h_in && t0 >= CH) {
+            // from the staged chunk holding slices [t0, t0 + n)
+            const int q = t0 / CH;
+            if ((e = cudaStreamWaitEvent(c->s_in, c->ev_dma[q], 0)) != cudaSuccess) break;
+            const char* src = (const char*)c->stage + (size_t)((int64_t)(q - 1) * R * 3 * P + (t0 - q * CH)) * esz;
+            if ((e = launch_pack(src, data_dtype, sst, g, buf, prec, 0, c->s_in, in_blocks)) != cudaSuccess) break;
+        } else if ((e = launch_pack((const char*)d_in + (size_t)t0 * esz, data_dtype, st, g, buf, prec, 0, c->s_in,
+                                    k == 0 ? 0u : in_blocks)) != cudaSuccess) {
             break;
+        }
         if ((e = cudaEventRecord(c->ev_in[j], c->s_in)) != cudaSuccess) break;
+        if (h_in && k == kdma) {
+            // chunks 1.. of the field, back to back on the copy stream once
+            // the first slabs have been read (before, the copies take the
+            // host link from the reads the first computes wait for)
+            if ((e = cudaStreamWaitEvent(c->s_dma, c->ev_in[j], 0)) != cudaSuccess) break;
+            for (int q = 1; q < nchunk && e == cudaSuccess; ++q) {
+                const int tq = q * CH, nq = NT - tq < CH ? NT - tq : CH;
+                for (int b = 0; b < 3 && e == cudaSuccess; ++b)
+                    for (int a = 0; a < R && e == cudaSuccess; ++a) {
+                        const char* hs = (const char*)h_in + (size_t)(4 * V * (a + 3 * b) + tq) * esz;
+                        char* dst = (char*)c->stage + (size_t)((q - 1) * R * 3 * P + (a + (int64_t)R * b) * P) * esz;
+                        e = cudaMemcpy2DAsync(dst, (size_t)CH * esz, hs, (size_t)NT * esz, (size_t)nq * esz,
+                                              (size_t)(4 * V3), cudaMemcpyHostToDevice, c->s_dma);
+                    }
+                if (e == cudaSuccess) e = cudaEventRecord(c->ev_dma[q], c->s_dma);
+            }
+            if (e != cudaSuccess) break;
+        }
         // compute slab k once it is packed and the output of slab k - nslot
         // has left this slot's workspace
         if ((e = cudaStreamWaitEvent(cs, c->ev_in[j], 0)) != cudaSuccess) break;
@@ -757,6 +862,28 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
             break;
         if ((e = cudaEventRecord(c->ev_cp[j], cs)) != cudaSuccess) break;
         if (!d_grad) continue;
+        if (t0 < Tdma) {
+            // gradient into the chunk buffer on the compute stream, once the
+            // copy of the chunk two before has left it; the chunk's copy
+            // follows its last slab
+            const int q = t0 / CH, tend = (q + 1) * CH < Tdma ? (q + 1) * CH : Tdma;
+            if (q >= 2 && (e = cudaStreamWaitEvent(cs, c->ev_dout[q - 2], 0)) != cudaSuccess) break;
+            char* ob = (char*)c->ostage + (size_t)(q % 2) * Bo;
+            if ((e = launch_energy_slab_out(U, ps, V, CH, t0 - q * CH, ob, form, buf + fbytes, wbytes, 0, cs,
+                                            data_dtype)) != cudaSuccess)
+                break;
+            if ((e = cudaEventRecord(c->ev_out[j], cs)) != cudaSuccess) break;
+            if ((e = cudaStreamWaitEvent(c->s_dout, c->ev_out[j], 0)) != cudaSuccess) break;
+            if (t0 + n == tend) {
+                e = cudaMemcpy2DAsync((char*)h_grad + (size_t)q * CH * esz, (size_t)NT * esz, ob, (size_t)CH * esz,
+                                      (size_t)(tend - q * CH) * esz, (size_t)(36 * V3), cudaMemcpyDeviceToHost,
+                                      c->s_dout);
+                if (e == cudaSuccess) e = cudaEventRecord(c->ev_dout[q], c->s_dout);
+                if (e != cudaSuccess) break;
+                last_dout = q;
+            }
+            continue;
+        }
         if ((e = cudaStreamWaitEvent(c->s_out, c->ev_cp[j], 0)) != cudaSuccess) break;
         const unsigned ob = k == nslab - 1 ? 0u : out_blocks;
         if ((e = launch_energy_slab_out(U, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, ob, c->s_out,
@@ -771,9 +898,12 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, int data_dtype, int 
         if (e == cudaSuccess) e = r;
     }
     if (e == cudaSuccess && d_grad) e = cudaStreamWaitEvent(c->st, c->ev_out[(nslab - 1) % nslot], 0);
+    if (e == cudaSuccess && last_dout >= 0) e = cudaStreamWaitEvent(c->st, c->ev_dout[last_dout], 0);
     if (e != cudaSuccess) {
+        cudaStreamSynchronize(c->s_dma);
         cudaStreamSynchronize(c->s_in);
         cudaStreamSynchronize(c->s_out);
+        cudaStreamSynchronize(c->s_dout);
         for (int i = 1; i < ncomp; ++i) cudaStreamSynchronize(c->s_cp[i - 1]);
         cudaStreamSynchronize(c->st);
         return cuda_status(e);
@@ -1012,7 +1142,9 @@ int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int 
     if (d_in && (!grad || d_grad)) {
         const int nslab = pipe_slabs(NT, V);
         if (nslab > 1)
-            return magnetic_force_pipelined(c, d_in, data_dtype, NT, NX, NY, NZ, prec, force_form, B, d_grad, nslab);
+            return magnetic_force_pipelined(c, d_in, pinned_host(data, "FLUE_DMA_IN") ? data : nullptr,
+                                            grad && pinned_host(grad, "FLUE_DMA_OUT") ? grad : nullptr, data_dtype,
+                                            NT, NX, NY, NZ, prec, force_form, B, d_grad, nslab);
     }
     flue_field U = {nullptr, NT, NX, NY, NZ, prec};
     // a complex128 field computed in FP32 (c128 data, prec C64 / R12) gets
@@ -1081,6 +1213,10 @@ void flue_release_host_cache(void) {
             c->slot[j] = nullptr;
             c->slot_bytes[j] = 0;
         }
+        if (c->stage) cudaFree(c->stage);
+        if (c->ostage) cudaFree(c->ostage);
+        c->stage = c->ostage = nullptr;
+        c->stage_bytes = c->ostage_bytes = 0;
     }
 }
 

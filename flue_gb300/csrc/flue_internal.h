@@ -92,12 +92,13 @@ cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, 
 // (B^2), where time slices are independent.  Part 1 (lines, forward, *out_E
 // normalised by vfull, line cotangents when with_force) computes the slab of
 // time slices [t0, t0 + nts) of field U (the whole field, or a packed slab
-// with t0 = 0).  Part 2 (link cotangents into the full-lattice gradient of
-// time extent ntf, grid capped at max_blocks per direction when > 0) takes U
-// with the slab's geometry (links unused) and writes the gradient as
-// out_dtype: the compute dtype, or complex128 (PREC_C128) from an FP32
-// computation.  Both use the same workspace, sized for the slab, and may run
-// on different streams.
+// with t0 = 0).  Part 2 (link cotangents, grid capped at max_blocks per
+// direction when > 0) takes U with the slab's geometry (links unused) and
+// writes the slab's gradient, normalised by vfull, at slices [t0, t0 + nts)
+// of an array of time extent ntf (the whole lattice's gradient, or a chunk
+// of time slices of it) as out_dtype: the compute dtype, or complex128
+// (PREC_C128) from an FP32 computation.  Both use the same workspace, sized
+// for the slab, and may run on different streams.
 cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const PlaneSet& ps, int64_t vfull,
                                    double* out_E, bool with_force, void* ws, size_t ws_bytes, cudaStream_t st);
 cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,

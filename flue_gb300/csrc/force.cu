@@ -721,12 +721,16 @@ cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_
     const PlaneArg pa = make_planes(ps);
     const EnergyWs w = energy_layout(U.g, U.prec, pa, true);
     if (ws_bytes < w.total) return cudaErrorInvalidValue;
+    // the gradient array: time extent ntf, the slab's spatial extents (the
+    // whole lattice's gradient, or a chunk of ntf time slices of it); vfull
+    // only normalises
+    const int64_t vout = (int64_t)ntf * (U.g.V / U.g.n[0]);
     if (U.prec == PREC_C128) {
         if (out_dtype != PREC_C128) return cudaErrorInvalidValue;
-        RefOut<double> fo{(double2*)force, vfull, 4, U.g.n[0], ntf, t0};
+        RefOut<double> fo{(double2*)force, vout, 4, U.g.n[0], ntf, t0};
         return energy_out_part<double>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
     }
-    RefOut<float> fo{(float2*)force, vfull, 4, U.g.n[0], ntf, t0};
+    RefOut<float> fo{(float2*)force, vout, 4, U.g.n[0], ntf, t0};
     if (out_dtype == PREC_C128) fo.p = nullptr, fo.pd = (double2*)force;
     return energy_out_part<float>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
 }

@@ -173,6 +173,49 @@ def test_host_buffer_force_time_slabs(prec_name, data_name, monkeypatch):
     assert abs(b.value - b1) < 1e-12 * abs(b1)
 
 
+@pytest.mark.parametrize("prec_name,data_name,slabs", [("r12", "c128", 10), ("r12", "c128", 14), ("c64", "c128", 10),
+                                                       ("c128", "c128", 13), ("r12", "c64", 20), ("c64", "c64", 7)])
+def test_host_buffer_force_dma_chunks(prec_name, data_name, slabs, monkeypatch):
+    """Pinned host buffers move by copy-engine copies of time-slice chunks
+    (FLUE_DMA_CHUNK slices rounded up to whole slabs; several chunks here, the
+    last one short, slabs of uneven length): the field in after its first
+    chunk, the gradient out before its last slabs (FLUE_OUT_TAIL of them, 0 =
+    none).  Every mix of copies and kernel reads / writes gives the
+    single-pass call's gradient bit for bit."""
+    import ctypes
+
+    from flue_gb300 import _lib
+
+    dims = (40, 4, 6, 4)
+    U = generate.random_field(dims, 0.4, 12)
+    dt = np.complex128 if data_name == "c128" else np.complex64
+    host = torch.as_tensor(np.asfortranarray(U.astype(dt))).permute(6, 5, 4, 3, 2, 1, 0).contiguous().pin_memory()
+    L = _lib.load()
+    code = {"c64": _lib.C64, "r12": _lib.R12, "c128": _lib.C128}[prec_name]
+    src = _lib.C128 if data_name == "c128" else _lib.C64
+
+    def run(nslab, dma_in, dma_out="1", tail="4", chunk="16"):
+        monkeypatch.setenv("FLUE_SLABS", str(nslab))
+        monkeypatch.setenv("FLUE_DMA_IN", dma_in)
+        monkeypatch.setenv("FLUE_DMA_OUT", dma_out)
+        monkeypatch.setenv("FLUE_OUT_TAIL", tail)
+        monkeypatch.setenv("FLUE_DMA_CHUNK", chunk)
+        grad = torch.full_like(host, float("nan")).pin_memory()
+        b = ctypes.c_double()
+        rc = L.flue_magnetic_force_c(ctypes.c_void_p(host.data_ptr()), src, *dims, code, _lib.FORCE_LIE,
+                                     ctypes.byref(b), ctypes.c_void_p(grad.data_ptr()))
+        assert rc == 0, L.flue_last_error_detail()
+        return b.value, grad.numpy().copy()
+
+    b1, g1 = run(1, "1")
+    assert np.isfinite(g1).all()
+    for mode in (("1", "1", "4"), ("1", "1", "0"), ("1", "1", "1"), ("0", "1", "2"), ("1", "0"), ("0", "0"),
+                 ("1", "1", "2", "5"), ("1", "1", "0", "32")):
+        b, g = run(slabs, *mode)
+        assert np.array_equal(g, g1), mode
+        assert abs(b - b1) < 1e-12 * abs(b1), mode
+
+
 @pytest.mark.parametrize("slabs,streams", [(2, 2), (3, 4), (8, 3), (8, 1)])
 def test_device_force_time_slabs(slabs, streams, monkeypatch):
     """The device B^2 force over time slabs on several streams equals the
