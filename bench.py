@@ -201,7 +201,7 @@ def bench_config(args, dims, n_replicas):
     return {"workload": f"5-loop F_munu + B^2 forward + backward (su(3) gradient), {nx}^3x{nt}",
             "lattice": [nt, nx, ny, nz], "sites": nt * nx * ny * nz, "field_format": args.prec, "eps": args.eps,
             "seed": args.seed, "global_batch": n_replicas, "parallelism": f"replicas x{n_replicas}",
-            "l2": "inputs and intermediates larger than L2 (field 0.4-0.6 GB, 8 GB DRAM traffic per step)"}
+            "l2": "inputs and intermediates larger than L2 (field 0.4-0.6 GB, 9 GB DRAM traffic per step)"}
 
 
 def ensemble_bench(steps: int):
@@ -426,9 +426,12 @@ def run_reference(args, dims, ws, rank):
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes (read + write) per site of one device step, from the ncu capture of this bench
-# (profiles/dram_traffic_b2_step_32x64.md: 16 time slabs at 32^3x64, reconstruct-12).
-TRAFFIC_PER_SITE = {("r12", (64, 32, 32, 32)): 3886.5}
+# DRAM bytes (read + write) per site of one device step, from an ncu capture of this bench
+# (16 time slabs at 32^3x64, reconstruct-12) with --cache-control none: no cache flush
+# between the kernels, so the write-backs of the intermediates (lines, F, line
+# cotangents) count where they happen.  ncu's default flush before every kernel writes
+# them back outside any kernel and the per-kernel sum then reads 3886.5 B/site.
+TRAFFIC_PER_SITE = {("r12", (64, 32, 32, 32)): 4358.6}
 
 
 def step_traffic(prec, dims):
