@@ -8,7 +8,9 @@
 #include <string.h>
 
 #include <atomic>
+#include <memory>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/flue_gb300.h"
@@ -706,8 +708,47 @@ int pipe_slabs(int NT, int64_t V) {
     return s < 1 ? 1 : s;
 }
 
+// Host memory that the CPU may write (pinned or pageable; not device or
+// managed memory).
+static bool cpu_writable(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeUnregistered;
+}
+
+// Zero-fills the listed byte ranges of host memory on up to 8 threads,
+// started at construction and joined at destruction.
+struct HostZeroFill {
+    std::vector<std::thread> th;
+    HostZeroFill(std::vector<std::pair<char*, size_t>> ranges) {
+        size_t total = 0;
+        for (auto& r : ranges) total += r.second;
+        unsigned hw = std::thread::hardware_concurrency();
+        const size_t nt = hw == 0 ? 4 : (hw < 8 ? hw : 8);
+        const size_t per = (total + nt - 1) / nt;
+        // thread k zeroes bytes [k * per, (k + 1) * per) of the ranges laid end to end
+        for (size_t k = 0; k < nt && per; ++k) {
+            th.emplace_back([ranges, per, k] {
+                size_t lo = k * per, hi = lo + per, at = 0;
+                for (auto& r : ranges) {
+                    const size_t a = lo > at ? lo : at, b = hi < at + r.second ? hi : at + r.second;
+                    if (a < b) memset(r.first + (a - at), 0, b - a);
+                    at += r.second;
+                }
+            });
+        }
+    }
+    ~HostZeroFill() {
+        for (auto& t : th) t.join();
+    }
+};
+
 int magnetic_force_pipelined(DevCache* c, const void* d_in, const void* h_in, void* h_grad, int data_dtype, int NT,
-                             int NX, int NY, int NZ, int prec, int form, double* B, void* d_grad, int nslab) {
+                             int NX, int NY, int NZ, int prec, int form, double* B, void* d_grad, int nslab,
+                             void* cpu_grad) {
     int rc = pipe_setup(c);
     if (rc) return rc;
     const int64_t V = (int64_t)NT * NX * NY * NZ;
@@ -806,6 +847,21 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, const void* h_in, vo
     // run on the whole GPU (8 slabs: 11.95 -> 11.79 ms per call).
     const unsigned in_blocks = (unsigned)env_int("FLUE_IN_BLOCKS", 32);
     const unsigned out_blocks = (unsigned)env_int("FLUE_OUT_BLOCKS", 16);
+    // B^2 has no plane with the time direction: its links are not packed
+    // (pmu0 = 1) and its gradient is zero.  With the gradient in host memory
+    // the CPU writes those zeros while the GPU computes, so that only the
+    // spatial directions cross the host link, 3/4 of the bytes each way
+    // (FLUE_HOST_ZERO=0: the GPU writes them; with copy-engine output too).
+    // Measured at 64x32^3 r12, same box, median per call: complex128 11.25 ms
+    // -> 10.94 (spatial pack) -> 9.66 (and host zeros); complex64 9.39 ->
+    // 9.16 ms.
+    const int pmu0 = 1;
+    std::unique_ptr<HostZeroFill> zfill;
+    if (cpu_grad && d_grad && !Tdma && env_int("FLUE_HOST_ZERO", 1)) {
+        std::vector<std::pair<char*, size_t>> r;
+        for (int ab = 0; ab < 9; ++ab) r.push_back({(char*)cpu_grad + (size_t)(4 * V * ab) * esz, (size_t)V * esz});
+        zfill.reset(new HostZeroFill(r));
+    }
     cudaError_t e = cudaEventRecord(c->ev_go, c->st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_in, c->ev_go, 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->s_out, c->ev_go, 0);
@@ -829,9 +885,9 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, const void* h_in, vo
             const int q = t0 / CH;
             if ((e = cudaStreamWaitEvent(c->s_in, c->ev_dma[q], 0)) != cudaSuccess) break;
             const char* src = (const char*)c->stage + (size_t)((int64_t)(q - 1) * R * 3 * P + (t0 - q * CH)) * esz;
-            if ((e = launch_pack(src, data_dtype, sst, g, buf, prec, 0, c->s_in, in_blocks)) != cudaSuccess) break;
+            if ((e = launch_pack(src, data_dtype, sst, g, buf, prec, 0, c->s_in, in_blocks, pmu0)) != cudaSuccess) break;
         } else if ((e = launch_pack((const char*)d_in + (size_t)t0 * esz, data_dtype, st, g, buf, prec, 0, c->s_in,
-                                    k == 0 ? 0u : in_blocks)) != cudaSuccess) {
+                                    k == 0 ? 0u : in_blocks, pmu0)) != cudaSuccess) {
             break;
         }
         if ((e = cudaEventRecord(c->ev_in[j], c->s_in)) != cudaSuccess) break;
@@ -846,8 +902,9 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, const void* h_in, vo
                     for (int a = 0; a < R && e == cudaSuccess; ++a) {
                         const char* hs = (const char*)h_in + (size_t)(4 * V * (a + 3 * b) + tq) * esz;
                         char* dst = (char*)c->stage + (size_t)((q - 1) * R * 3 * P + (a + (int64_t)R * b) * P) * esz;
-                        e = cudaMemcpy2DAsync(dst, (size_t)CH * esz, hs, (size_t)NT * esz, (size_t)nq * esz,
-                                              (size_t)(4 * V3), cudaMemcpyHostToDevice, c->s_dma);
+                        e = cudaMemcpy2DAsync(dst + (size_t)V3 * CH * esz, (size_t)CH * esz, hs + (size_t)V * esz,
+                                              (size_t)NT * esz, (size_t)nq * esz, (size_t)(3 * V3),
+                                              cudaMemcpyHostToDevice, c->s_dma);
                     }
                 if (e == cudaSuccess) e = cudaEventRecord(c->ev_dma[q], c->s_dma);
             }
@@ -887,7 +944,7 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, const void* h_in, vo
         if ((e = cudaStreamWaitEvent(c->s_out, c->ev_cp[j], 0)) != cudaSuccess) break;
         const unsigned ob = k == nslab - 1 ? 0u : out_blocks;
         if ((e = launch_energy_slab_out(U, ps, V, NT, t0, d_grad, form, buf + fbytes, wbytes, ob, c->s_out,
-                                        data_dtype)) != cudaSuccess)
+                                        data_dtype, zfill != nullptr)) != cudaSuccess)
             break;
         if ((e = cudaEventRecord(c->ev_out[j], c->s_out)) != cudaSuccess) break;
     }
@@ -1144,7 +1201,8 @@ int flue_magnetic_force_c(const void* data, int data_dtype, int NT, int NX, int 
         if (nslab > 1)
             return magnetic_force_pipelined(c, d_in, pinned_host(data, "FLUE_DMA_IN") ? data : nullptr,
                                             grad && pinned_host(grad, "FLUE_DMA_OUT") ? grad : nullptr, data_dtype,
-                                            NT, NX, NY, NZ, prec, force_form, B, d_grad, nslab);
+                                            NT, NX, NY, NZ, prec, force_form, B, d_grad, nslab,
+                                            grad && cpu_writable(grad) ? grad : nullptr);
     }
     flue_field U = {nullptr, NT, NX, NY, NZ, prec};
     // a complex128 field computed in FP32 (c128 data, prec C64 / R12) gets

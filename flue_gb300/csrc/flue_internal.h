@@ -42,9 +42,10 @@ cudaError_t launch_finish_sums(const double* partial, int nparts, int nout, doub
                                double scale = 1.0);
 
 // layouts
-// max_blocks > 0 caps the grid (the kernel is grid-strided)
+// max_blocks > 0 caps the grid (the kernel is grid-strided); mu0 > 0 packs
+// only the directions mu0..3 (the others are left as they are)
 cudaError_t launch_pack(const void* src, int src_dtype, const int64_t strides[7], const Geom& g, void* dst, int dst_prec,
-                        int reunitarise, cudaStream_t st, unsigned max_blocks = 0);
+                        int reunitarise, cudaStream_t st, unsigned max_blocks = 0, int mu0 = 0);
 cudaError_t launch_unpack(const FieldRef& U, void* dst, int dst_dtype, cudaStream_t st);
 cudaError_t launch_matmul_batch(const void* l, const void* r, void* o, int64_t n, int dtype, int dagger, cudaStream_t st);
 cudaError_t launch_fix_field(void* links, const Geom& g, int prec, cudaStream_t st);
@@ -101,9 +102,11 @@ cudaError_t launch_energy(const FieldRef& U, const PlaneSet& ps, double* out_E, 
 // for the slab, and may run on different streams.
 cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const PlaneSet& ps, int64_t vfull,
                                    double* out_E, bool with_force, void* ws, size_t ws_bytes, cudaStream_t st);
+// skip_zero: the directions without a plane (zero gradient) are not written
+// (the caller fills them).
 cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
                                    int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st,
-                                   int out_dtype);
+                                   int out_dtype, bool skip_zero = false);
 // launch_energy over nslab time slabs on nstream (<= 4) streams forked from
 // st (plane sets without the time direction); workspace of
 // energy_slabs_ws_bytes(...) bytes.  Results equal launch_energy's: the

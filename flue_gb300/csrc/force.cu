@@ -480,9 +480,11 @@ __global__ void __launch_bounds__(COT_BS, MinBlocks<T>::cot)
 //    beside other kernels
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_linkcot(Geom g, PlaneArg pa, MatAoS<T> lines, MatAoS<T> lam, T scale, int form, RefOut<T> out) {
+__global__ void k_linkcot(Geom g, PlaneArg pa, MatAoS<T> lines, MatAoS<T> lam, T scale, int form, RefOut<T> out,
+                          bool skip_zero) {
     const int d = blockIdx.y;
     const int slot = sel(pa.slot, d);
+    if (slot < 0 && skip_zero) return;
     for (int64_t z = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; z < g.V; z += (int64_t)gridDim.x * blockDim.x) {
         if (slot < 0) {
             out.store(z, d, m_zero<T>());
@@ -658,13 +660,14 @@ static cudaError_t energy_fwd_part(const L& U, const Geom& g, const Geom& gs, in
 // Part 2: link cotangents, gradient of E/vnorm written through `fo`.
 template <typename T>
 static cudaError_t energy_out_part(const Geom& g, const PlaneArg& pa, double vnorm, int form, char* ws,
-                                   const EnergyWs& w, RefOut<T> fo, unsigned max_blocks, cudaStream_t st) {
+                                   const EnergyWs& w, RefOut<T> fo, unsigned max_blocks, cudaStream_t st,
+                                   bool skip_zero = false) {
     MatAoS<T> lines{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lines), g.V};
     MatAoS<T> lam{reinterpret_cast<decltype(MatAoS<T>::p)>(ws + w.lam), g.V};
     const T scale = (T)(-1.0 / (2.0 * vnorm));
     unsigned nb = (unsigned)((g.V + 127) / 128);
     if (max_blocks && nb > max_blocks) nb = max_blocks;
-    note_launch(), k_linkcot<T><<<dim3(nb, 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo);
+    note_launch(), k_linkcot<T><<<dim3(nb, 4), 128, 0, st>>>(g, pa, lines, lam, scale, form, fo, skip_zero);
     stage_mark(4, st);
     return cudaGetLastError();
 }
@@ -716,7 +719,7 @@ cudaError_t launch_energy_slab_fwd(const FieldRef& U, int t0, int nts, const Pla
 
 cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_t vfull, int ntf, int t0, void* force,
                                    int force_form, void* ws, size_t ws_bytes, unsigned max_blocks, cudaStream_t st,
-                                   int out_dtype) {
+                                   int out_dtype, bool skip_zero) {
     if (has_time_plane(ps) || vfull < U.g.V || t0 < 0 || t0 + U.g.n[0] > ntf) return cudaErrorInvalidValue;
     const PlaneArg pa = make_planes(ps);
     const EnergyWs w = energy_layout(U.g, U.prec, pa, true);
@@ -728,11 +731,12 @@ cudaError_t launch_energy_slab_out(const FieldRef& U, const PlaneSet& ps, int64_
     if (U.prec == PREC_C128) {
         if (out_dtype != PREC_C128) return cudaErrorInvalidValue;
         RefOut<double> fo{(double2*)force, vout, 4, U.g.n[0], ntf, t0};
-        return energy_out_part<double>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
+        return energy_out_part<double>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st,
+                                       skip_zero);
     }
     RefOut<float> fo{(float2*)force, vout, 4, U.g.n[0], ntf, t0};
     if (out_dtype == PREC_C128) fo.p = nullptr, fo.pd = (double2*)force;
-    return energy_out_part<float>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st);
+    return energy_out_part<float>(U.g, pa, (double)vfull, force_form, (char*)ws, w, fo, max_blocks, st, skip_zero);
 }
 
 // ---------------------------------------------------------------------------

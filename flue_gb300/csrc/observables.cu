@@ -111,24 +111,26 @@ __device__ __forceinline__ void pack_one(const SRC* __restrict__ src, const Stri
 }
 
 template <typename SRC>
-__global__ void k_pack(const SRC* __restrict__ src, Strides7 sd, Geom g, void* __restrict__ dst, int dst_prec, int reun) {
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < 4 * g.V;
+__global__ void k_pack(const SRC* __restrict__ src, Strides7 sd, Geom g, void* __restrict__ dst, int dst_prec, int reun,
+                       int mu0) {
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (4 - mu0) * g.V;
          idx += (int64_t)gridDim.x * blockDim.x)
-        pack_one(src, sd, g, dst, dst_prec, reun, idx);
+        pack_one(src, sd, g, dst, dst_prec, reun, idx + mu0 * g.V);
 }
 
 cudaError_t launch_pack(const void* src, int src_dtype, const int64_t strides[7], const Geom& g, void* dst, int dst_prec,
-                        int reunitarise, cudaStream_t st, unsigned max_blocks) {
+                        int reunitarise, cudaStream_t st, unsigned max_blocks, int mu0) {
     Strides7 sd;
     for (int k = 0; k < 7; ++k) sd.s[k] = strides[k];
-    const int64_t n = 4 * g.V;
+    if (mu0 < 0 || mu0 > 3) return cudaErrorInvalidValue;
+    const int64_t n = (4 - mu0) * g.V;
     const int bs = 256;
     unsigned nb = (unsigned)((n + bs - 1) / bs);
     if (max_blocks && nb > max_blocks) nb = max_blocks;
     if (src_dtype == PREC_C128)
-        note_launch(), k_pack<double2><<<nb, bs, 0, st>>>((const double2*)src, sd, g, dst, dst_prec, reunitarise);
+        note_launch(), k_pack<double2><<<nb, bs, 0, st>>>((const double2*)src, sd, g, dst, dst_prec, reunitarise, mu0);
     else
-        note_launch(), k_pack<float2><<<nb, bs, 0, st>>>((const float2*)src, sd, g, dst, dst_prec, reunitarise);
+        note_launch(), k_pack<float2><<<nb, bs, 0, st>>>((const float2*)src, sd, g, dst, dst_prec, reunitarise, mu0);
     return cudaGetLastError();
 }
 

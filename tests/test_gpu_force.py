@@ -165,6 +165,11 @@ def test_host_buffer_force_time_slabs(prec_name, data_name, monkeypatch):
         b, g = run(slabs)
         assert abs(b - b1) < 1e-12 * abs(b1), slabs
         assert np.array_equal(g, g1), slabs
+    # the zero time-direction gradient written by the GPU instead of host threads
+    monkeypatch.setenv("FLUE_HOST_ZERO", "0")
+    b, g = run(3)
+    assert np.array_equal(g, g1)
+    monkeypatch.delenv("FLUE_HOST_ZERO")
     # B^2 alone (no gradient) through the pipeline
     monkeypatch.setenv("FLUE_SLABS", "4")
     b = ctypes.c_double()
