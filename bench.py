@@ -623,6 +623,15 @@ def main():
     e2e_val = wsz * V / e2e_s
     e2e64_s, h2d64 = e2e_leg(torch.complex64, _lib.C64)
 
+    def link_bytes(esz):
+        # what crosses the host link per call: B^2 reads the spatial links
+        # (their stored rows: 2 of 3 for reconstruct-12) and writes the
+        # spatial gradient; host threads write the zero time-direction part
+        rows = 2 if args.prec == "r12" else 3
+        return {"h2d": 3 * rows * 3 * V * esz, "d2h": 27 * V * esz,
+                "note": "spatial links (stored rows) in, spatial gradient out; the zero time-direction gradient "
+                        "is written into the caller's buffer by host threads"}
+
     # --- CPU baseline (rank 0, N = 1 only) ---
     cpu = None
     cpu_b2 = None
@@ -678,11 +687,11 @@ def main():
                                       "precision, the same work as the CPU figures"},
         "gpu_launches": int(n_launches),
         "e2e": {"value": e2e_val, "unit": "sites/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d + 8,
-                "s_per_step": e2e_s,
+                "s_per_step": e2e_s, "host_link_bytes_per_step": link_bytes(16),
                 "api": f"flue_magnetic_force_c (host complex128 field in, {args.prec} FP32 compute, host complex128 "
                        "gradient out)"},
         "e2e_c64": {"value": wsz * V / e2e64_s, "unit": "sites/s", "h2d_bytes_per_step": h2d64,
-                    "d2h_bytes_per_step": h2d64 + 8, "s_per_step": e2e64_s,
+                    "d2h_bytes_per_step": h2d64 + 8, "s_per_step": e2e64_s, "host_link_bytes_per_step": link_bytes(8),
                     "api": f"flue_magnetic_force_c (host complex64 field in, {args.prec} FP32 compute, host "
                            "complex64 gradient out)"},
         "roofline": {"bound": "hbm", "kernel": "whole fwd+bwd step (metric's %HBM)", "achieved": achieved_gbs,
