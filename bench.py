@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--eps", type=float, default=0.3)
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--fp64-steps", type=int, default=3)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--ensemble", action="store_true",
@@ -608,7 +608,8 @@ def main():
             if rc:
                 raise RuntimeError(L.flue_last_error_detail().decode())
 
-        e2e_step()
+        for _ in range(3):
+            e2e_step()
         barrier(wsz)
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
