@@ -1,0 +1,158 @@
+"""Golden vectors from the reference's own Fortran, run through a translator.
+
+No Fortran compiler is available, so `fortran_subset.py` translates the
+reference's `src/constants.f90`, `src/SU3MatrixOps.f90`, `src/wloops.F90` and
+the FixSU3Matrix routines of `src/gaugeIO/ILDG_bin.f90` statement by statement into Python over numpy (in memory) and runs the
+routines as written (serial build: no OpenMP / `do concurrent` macros) on the
+fields below.  Their outputs are stored in `reference_fortran.json` with the
+recipe of every input, so that the oracle (CPU) and the CUDA library (GPU)
+are compared with the reference's own code paths, not only with a
+restatement of them.
+
+Inputs: seeded fields of `flue_gb300.generate` (numpy PCG64: `random_field`
+= exp(i eps H) links, `haar_field` = Haar-random SU(3)), rebuilt by the
+tests from the recipe and checked against the stored checksums; random 3x3
+complex matrices drawn from PCG64 and stored as they are.
+
+Run in a container that holds the reference tree (it is read, never
+copied):
+    python tests/golden/make_reference_golden.py [/path/to/reference]
+The config-0 field (8^3 x 16) takes several minutes in the translated
+routines.
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from flue_gb300 import generate  # noqa: E402
+from tests.golden import fortran_subset  # noqa: E402
+
+OUT = os.path.join(HERE, "reference_fortran.json")
+SOURCES = ("src/constants.f90", "src/SU3MatrixOps.f90", "src/wloops.F90", "src/gaugeIO/ILDG_bin.f90")
+# file readers (Fortran I/O statements): outside the translated subset, not run
+SKIP = ("readgaugefield_ildg", "readgaugetransformation_cola")
+
+
+def field(recipe):
+    if recipe["kind"] == "random":
+        return generate.random_field(tuple(recipe["dims"]), recipe["eps"], recipe["seed"])
+    if recipe["kind"] == "haar":
+        return generate.haar_field(tuple(recipe["dims"]), recipe["seed"])
+    raise ValueError(recipe["kind"])
+
+
+def checksum(U):
+    """Sum of |U|^2 and a weighted sum that depends on every element's place."""
+    w = np.cos(np.arange(U.size, dtype=np.float64) * 0.61803398875).reshape(U.shape, order="F")
+    return [float(np.sum(np.abs(U) ** 2)), float(np.sum(w * U.real)), float(np.sum(w * U.imag))]
+
+
+def cplx(a):
+    a = np.asarray(a)
+    return [np.real(a).ravel(order="F").tolist(), np.imag(a).ravel(order="F").tolist()]
+
+
+def field_summary(F):
+    """An F field (NT,NX,NY,NZ,3,3): its checksum and the matrices at 12
+    sites spread over the lattice (linear site index, time fastest)."""
+    V = int(np.prod(F.shape[:4]))
+    flat = F.reshape((V, 3, 3), order="F")
+    sites = sorted({int(round(k * (V - 1) / 11)) for k in range(12)})
+    return {"checksum": checksum(F), "sites": {str(k): cplx(flat[k]) for k in sites}}
+
+
+# observables per field; "full" adds the clover and 5-loop F fields (their
+# checksums and 12 sites each; small lattices only)
+CASES = [
+    {"name": "random_4x3x4x3", "recipe": {"kind": "random", "dims": [4, 3, 4, 3], "eps": 0.4, "seed": 5},
+     "full": True},
+    {"name": "haar_3x4x2x3", "recipe": {"kind": "haar", "dims": [3, 4, 2, 3], "seed": 7}, "full": True},
+    {"name": "config0_8x8x8x16", "recipe": {"kind": "random", "dims": [16, 8, 8, 8], "eps": 0.3, "seed": 1},
+     "full": False},
+]
+# (coordinates inside every lattice below: t, x, z <= 3, y <= 2)
+PATHS = [
+    ([1, 1, 1, 1], [1, 2, -1, -2]),
+    ([2, 3, 1, 2], [2, 3, -2, -3, 4, 4, -4, -4]),
+    ([3, 2, 2, 1], [-1, -3, 2, 1, 3, -2]),
+    ([1, 3, 2, 3], [4, 4, 4, 1, -4, -4, -4, -1]),
+]
+WLOOPS = [(2, 3, 1, 1), (2, 3, 2, 1), (3, 4, 1, 3), (1, 2, 2, 2), (4, 2, 3, 2)]
+WLOOPS_TAU = [(1, 2, 3, 1, 2), (2, 3, 4, 2, 2)]
+PLANES = [(3, 2), (2, 4), (4, 3), (1, 2)]
+
+
+def run_case(ns, case, log):
+    U = field(case["recipe"])
+    NT, NX, NY, NZ = U.shape[:4]
+    out = {"recipe": case["recipe"], "checksum": checksum(U)}
+    t = time.time()
+    plaq = {}
+    for rng in ((1, 4, 4), (2, 4, 4), (1, 1, 4)):
+        s, n, _ = ns["plaquette"](U, *rng, 0.0, 0, 0.0)
+        sg, ng, _ = ns["genplaquette"](U, NT, NX, NY, NZ, *rng, 0.0, 0, 0.0)
+        plaq[",".join(map(str, rng))] = {"sum": s, "n": int(n), "gen_sum": sg, "gen_n": int(ng)}
+    out["plaquette"] = plaq
+    s, n, _ = ns["polyakov"](U, 0.0, 0, 0.0)
+    out["polyakov"] = {"sum": s, "n": int(n)}
+    out["genericpath"] = [{"coord": c, "path": p, "matrix": cplx(ns["genericpath"](U, np.array(c), np.array(p)))}
+                          for c, p in PATHS]
+    out["wmunu"] = [{"args": list(a), "value": ns["wmunu"](U, *a)} for a in WLOOPS]
+    out["wmunutau"] = [{"args": list(a), "value": ns["wmunutau"](U, *a)} for a in WLOOPS_TAU]
+    log(f"  {case['name']}: plaquette, polyakov, paths, loops {time.time() - t:.1f} s")
+    if case["full"]:
+        out["clover"] = [dict(plane=list(pl), **field_summary(ns["cloverloopmunucoord"](U, NT, NX, NY, NZ, *pl)))
+                         for pl in PLANES[:2]]
+        out["loop5"] = [dict(plane=list(pl), **field_summary(ns["loop5munucoord"](U, NT, NX, NY, NZ, *pl)))
+                        for pl in PLANES]
+        log(f"  {case['name']}: clover and 5-loop F {time.time() - t:.1f} s")
+    out["magnetic"] = ns["magnetic"](U, NT, NX, NY, NZ)
+    log(f"  {case['name']}: magnetic {time.time() - t:.1f} s")
+    return out
+
+
+def main(ref_root):
+    tr = fortran_subset.Translator()
+    for rel in SOURCES:
+        with open(os.path.join(ref_root, rel)) as f:
+            tr.add_source(f.read())
+    ns = tr.build(only={n for n in tr.procs if n not in SKIP})
+
+    def log(msg):
+        print(msg, flush=True)
+
+    rng = np.random.Generator(np.random.PCG64(11))
+    mats = [(rng.standard_normal((3, 3)) + 1j * rng.standard_normal((3, 3))) for _ in range(4)]
+    zero33 = np.zeros((3, 3), dtype=np.complex128)
+    alg = {
+        "matrices": [cplx(m) for m in mats],
+        "multiplymatmat": cplx(ns["multiplymatmat"](zero33, mats[0], mats[1])[0]),
+        "multiplymatdagmatdag": cplx(ns["multiplymatdagmatdag"](zero33, mats[2], mats[3])[0]),
+        "realtracemultmatmat": ns["realtracemultmatmat"](0.0, mats[0], mats[3])[0],
+        "tracelessconjgsubtract": cplx(ns["tracelessconjgsubtract"](zero33, mats[1], mats[2])[0]),
+        "colourdecomp": cplx(ns["colourdecomp"](np.zeros(8, dtype=np.complex128), mats[3])[0]),
+    }
+    # FixSU3Matrix (re-unitarisation of a stored link): raw random matrices
+    # and Haar SU(3) matrices with a 1e-3 perturbation
+    haar = generate.haar_field((1, 1, 1, 1), 3)[0, 0, 0, 0]
+    fix_in = mats[:2] + [haar[k] + 1e-3 * (rng.standard_normal((3, 3)) + 1j * rng.standard_normal((3, 3)))
+                         for k in range(3)]
+    alg["fixsu3matrix"] = {"in": [cplx(m) for m in fix_in],
+                           "out": [cplx(ns["fixsu3matrix"](m.copy())[0]) for m in fix_in]}
+    res = {"sources": list(SOURCES), "algebra": alg, "fields": {}}
+    for case in CASES:
+        res["fields"][case["name"]] = run_case(ns, case, log)
+    with open(OUT, "w") as f:
+        json.dump(res, f, separators=(",", ":"))
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
