@@ -125,8 +125,9 @@ INTRINSICS = {
     "conjg": "np.conj", "transpose": "np.transpose", "abs": "abs", "aimag": "np.imag", "all": "_all",
     "shape": "_shape", "size": "_size", "real": "_real", "cmplx": "_cmplx", "reshape": "_reshape",
     "acos": "np.arccos", "sqrt": "np.sqrt", "exp": "np.exp", "cos": "np.cos", "sin": "np.sin",
-    "sum": "np.sum", "mod": "_mod", "modulo": "_modulo", "int": "_int", "dble": "float", "max": "max",
-    "min": "min",
+    "sum": "_sum", "mod": "_mod", "modulo": "_modulo", "int": "_int", "dble": "float", "max": "max",
+    "min": "min", "maxval": "_maxval", "minval": "_minval", "any": "_any", "count": "_count", "pack": "_pack",
+    "dot_product": "_dot", "present": "_present",
 }
 
 
@@ -343,6 +344,45 @@ def _mod(a, b):
     return int(np.fmod(a, b))
 
 
+def _sum(a, dim=None, mask=None):
+    a = np.asarray(a)
+    if mask is not None:
+        return a[np.broadcast_to(mask, a.shape)].sum()
+    return a.sum() if dim is None else a.sum(axis=int(dim) - 1)
+
+
+def _maxval(a, mask=None):
+    a = np.asarray(a)
+    return (a[mask] if mask is not None else a).max()
+
+
+def _minval(a, mask=None):
+    a = np.asarray(a)
+    return (a[mask] if mask is not None else a).min()
+
+
+def _any(m):
+    return bool(np.any(m))
+
+
+def _count(m, kind=None):
+    return int(np.count_nonzero(m))
+
+
+def _pack(a, mask):
+    a = np.asarray(a)
+    return a.ravel(order="F")[np.broadcast_to(mask, a.shape).ravel(order="F")]
+
+
+def _dot(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.vdot(a, b) if np.iscomplexobj(a) else np.dot(a, b)
+
+
+def _present(x):
+    return x is not None
+
+
 def _modulo(a, b):
     return a % b  # (Python's % takes the sign of the divisor, as MODULO does)
 
@@ -365,24 +405,26 @@ def _arr(items):
     return np.array(flat, dtype=np.float64)
 
 
-def _ix(spec):
-    """Python index tuple from (kind, lo, hi) entries with 1-based bounds."""
+def _ix(spec, lbs=None):
+    """Python index tuple from (kind, lo, hi) entries, bounds relative to the
+    dimensions' lower bounds (1 unless given)."""
     out = []
-    for kind, lo, hi in spec:
+    for k, (kind, lo, hi) in enumerate(spec):
+        b = int(lbs[k]) if lbs is not None else 1
         if kind == "sec":
-            out.append(slice(None if lo is None else int(lo) - 1, None if hi is None else int(hi)))
+            out.append(slice(None if lo is None else int(lo) - b, None if hi is None else int(hi) - b + 1))
         else:
-            out.append(int(lo) - 1)
+            out.append(int(lo) - b)
     return tuple(out)
 
 
-def _get(a, *spec):
-    v = a[_ix(spec)]
+def _get(a, *spec, lbs=None):
+    v = a[_ix(spec, lbs)]
     return v.copy() if isinstance(v, np.ndarray) else v
 
 
-def _set(a, spec, val):
-    a[_ix(spec)] = val
+def _set(a, spec, val, lbs=None):
+    a[_ix(spec, lbs)] = val
 
 
 def _copy(v):
@@ -461,7 +503,7 @@ class Procedure:
                 if depth == 0:
                     break
             attrs = _split_top(rest[j + 1:].lstrip(",").strip()) if rest[j + 1:].strip() else []
-        dims, intent, param = None, None, False
+        dims, intent, param, optional = None, None, False, False
         for a in attrs:
             al = a.lower()
             if al.startswith("dimension"):
@@ -470,6 +512,8 @@ class Procedure:
                 intent = al[al.index("(") + 1:al.index(")")].strip()
             elif al == "parameter":
                 param = True
+            elif al == "optional":
+                optional = True
         for ent in _split_top(m.group(3)):
             init = None
             if "=" in ent and not ent.strip().startswith("("):
@@ -482,7 +526,19 @@ class Procedure:
             if "(" in nm:
                 edims = _split_top(nm[nm.index("(") + 1:nm.rindex(")")])
                 nm = nm[:nm.index("(")].strip()
-            self.decl[nm.lower()] = {"type": typ, "dims": edims, "intent": intent, "parameter": param, "init": init}
+            self.decl[nm.lower()] = {"type": typ, "dims": edims, "intent": intent, "parameter": param, "init": init,
+                                     "optional": optional}
+
+    def lbounds(self, name):
+        """Lower bounds of array `name` (expressions), or None when all are 1."""
+        d = self.decl.get(name)
+        if not d or not d["dims"]:
+            return None
+        lbs = []
+        for x in d["dims"]:
+            parts = _split_top(x, ":")
+            lbs.append(parts[0] if len(parts) == 2 and parts[0] else "1")
+        return None if all(v == "1" for v in lbs) else lbs
 
 
 class Translator:
@@ -505,6 +561,9 @@ class Translator:
                 in_contains = True
             elif low.startswith("end module"):
                 in_contains = False
+            elif low.startswith("interface") and not in_contains:
+                while not re.match(r"^end\s*interface\b", stmts[i], re.I):
+                    i += 1
             elif not in_contains:
                 m = _DECL.match(st)
                 if m:
@@ -537,10 +596,13 @@ class Translator:
                 return "v_" + name
 
             def apply(self, name, args):
-                if name in tr.procs:
+                declared = proc is not None and name in proc.decl and proc.decl[name]["dims"]
+                if name == "present":
+                    return f"_present({args[0][2]})"
+                if name in tr.procs and not declared:
                     pos = [tr._argval(a, self) for a in args]
                     return f"{name}({', '.join(pos)})"
-                if name in INTRINSICS:
+                if name in INTRINSICS and not declared:
                     parts = []
                     for kind, lo, hi in args:
                         if kind == "kw":
@@ -555,7 +617,9 @@ class Translator:
                         spec.append(f"('sec', {lo}, {hi})")
                     else:
                         spec.append(f"('pos', {hi}, None)")
-                return f"_get(v_{name}, {', '.join(spec)})"
+                lbs = proc.lbounds(name) if proc is not None else None
+                lb = f", lbs=({', '.join(lbs)},)" if lbs else ""
+                return f"_get(v_{name}, {', '.join(spec)}{lb})"
 
         return Ctx()
 
@@ -569,11 +633,13 @@ class Translator:
         return _Expr(s, ctx).parse()
 
     def _lhs(self, s, ctx):
-        """(name, spec) for an assignment target."""
+        """(name, spec) for an assignment target; spec ends with the lower
+        bounds keyword when the array has any other than 1."""
         s = s.strip()
         if "(" not in s:
             return "v_" + s.lower(), None
-        name = "v_" + s[:s.index("(")].strip().lower()
+        raw = s[:s.index("(")].strip().lower()
+        name = "v_" + raw
         inner = s[s.index("(") + 1:s.rindex(")")]
         ex = _Expr(inner, ctx)
         spec = []
@@ -582,6 +648,8 @@ class Translator:
             spec.append(f"('sec', {lo}, {hi})" if kind == "sec" else f"('pos', {hi}, None)")
             if ex.peek()[1] == ",":
                 ex.take()
+        lbs = self._proc.lbounds(raw) if getattr(self, "_proc", None) is not None else None
+        self._lhs_lbs = f", lbs=({', '.join(lbs)},)" if lbs else ""
         return name, spec
 
     def _assign_split(self, st):
@@ -597,7 +665,10 @@ class Translator:
 
     def emit(self, proc: Procedure) -> str:
         ctx = self._ctx(proc)
-        L = [f"def {proc.name}({', '.join('v_' + a for a in proc.args)}):"]
+        self._proc = proc
+        # (every dummy defaults to None: optional arguments may precede required ones)
+        sig = [f"v_{a}=None" for a in proc.args]
+        L = [f"def {proc.name}({', '.join(sig)}):"]
         ind = "    "
         for a in proc.args:  # copy-in of the dummies the procedure may change (copied out on return)
             if (proc.decl.get(a, {}).get("intent") or "inout") != "in":
@@ -615,7 +686,14 @@ class Translator:
             dt = {"complex": "np.complex128", "real": "np.float64", "integer": "np.int64",
                   "logical": "np.bool_", "character": "object"}[d["type"]]
             if d["dims"]:
-                shape = ", ".join(f"int({self._expr(x, ctx)})" for x in d["dims"])
+                ext = []
+                for x in d["dims"]:
+                    parts = _split_top(x, ":")
+                    if len(parts) == 2:
+                        ext.append(f"int({self._expr(parts[1], ctx)}) - int({self._expr(parts[0] or '1', ctx)}) + 1")
+                    else:
+                        ext.append(f"int({self._expr(x, ctx)})")
+                shape = ", ".join(ext)
                 L.append(f"{ind}v_{name} = np.zeros(({shape},), dtype={dt}, order='F')")
             else:
                 L.append(f"{ind}v_{name} = {dt}(0)" if dt != "object" else f"{ind}v_{name} = ''")
@@ -629,6 +707,14 @@ class Translator:
                 step = self._expr(bounds[2], ctx) if len(bounds) > 2 else "1"
                 L.append(f"{ind}for v_{m.group(1).lower()} in range(int({lo}), int({hi}) + (1 if {step} > 0 else -1),"
                          f" int({step})):")
+                ind += "    "
+                stack.append("do")
+                continue
+            if low == "do" or re.match(r"^do\s+while\b", low):
+                cond = "True"
+                if low != "do":
+                    cond = self._expr(st[st.index("(") + 1:st.rindex(")")], ctx)
+                L.append(f"{ind}while {cond}:")
                 ind += "    "
                 stack.append("do")
                 continue
@@ -705,6 +791,10 @@ class Translator:
         low = st.lower()
         if low == "stop" or low.startswith("stop "):
             return [f"{ind}_stop()"]
+        if low == "exit":
+            return [f"{ind}break"]
+        if low == "cycle":
+            return [f"{ind}continue"]
         if low == "return":
             raise SyntaxError("return is outside the translated subset")
         m = re.match(r"^call\s+(\w+)\s*(?:\((.*)\))?$", st, re.I)
@@ -721,11 +811,13 @@ class Translator:
             outs = [i for i, a in enumerate(proc.args)
                     if (proc.decl.get(a, {}).get("intent") or "inout") in ("out", "inout")]
             for k, i in enumerate(outs):
+                if i >= len(args):
+                    continue  # (an optional argument not passed)
                 tname, spec = self._lhs(args[i], ctx)
                 if spec is None:
                     lines.append(f"{ind}{tname} = _copy({tmp}[{k}])")
                 else:
-                    lines.append(f"{ind}_set({tname}, ({', '.join(spec)},), {tmp}[{k}])")
+                    lines.append(f"{ind}_set({tname}, ({', '.join(spec)},), {tmp}[{k}]{self._lhs_lbs})")
             return lines
         sp = self._assign_split(st)
         if sp is None:
@@ -735,7 +827,7 @@ class Translator:
         val = self._expr(rhs, ctx)
         if spec is None:
             return [f"{ind}{name} = _assign({name}, {val})"]
-        return [f"{ind}_set({name}, ({', '.join(spec)},), {val})"]
+        return [f"{ind}_set({name}, ({', '.join(spec)},), {val}{self._lhs_lbs})"]
 
     def build(self, only=None) -> dict:
         """Python namespace with the translated procedures (all, or the names

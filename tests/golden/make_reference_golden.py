@@ -1,8 +1,10 @@
 """Golden vectors from the reference's own Fortran, run through a translator.
 
 No Fortran compiler is available, so `fortran_subset.py` translates the
-reference's `src/constants.f90`, `src/SU3MatrixOps.f90`, `src/wloops.F90` and
-the FixSU3Matrix routines of `src/gaugeIO/ILDG_bin.f90` statement by statement into Python over numpy (in memory) and runs the
+reference's `src/constants.f90`, `src/SU3MatrixOps.f90`, `src/wloops.F90`,
+the FixSU3Matrix routines of `src/gaugeIO/ILDG_bin.f90` and the analysis
+helpers (`src/jack.f90`, `src/gluonAna/momentum.f90`,
+`src/gluonAna/gpManip.f90`) statement by statement into Python over numpy (in memory) and runs the
 routines as written (serial build: no OpenMP / `do concurrent` macros) on the
 fields below.  Their outputs are stored in `reference_fortran.json` with the
 recipe of every input, so that the oracle (CPU) and the CUDA library (GPU)
@@ -36,6 +38,7 @@ from tests.golden import fortran_subset  # noqa: E402
 
 OUT = os.path.join(HERE, "reference_fortran.json")
 SOURCES = ("src/constants.f90", "src/SU3MatrixOps.f90", "src/wloops.F90", "src/gaugeIO/ILDG_bin.f90")
+ANALYSIS_SOURCES = ("src/jack.f90", "src/gluonAna/momentum.f90", "src/gluonAna/gpManip.f90")
 # file readers (Fortran I/O statements): outside the translated subset, not run
 SKIP = ("readgaugefield_ildg", "readgaugetransformation_cola")
 
@@ -118,6 +121,63 @@ def run_case(ns, case, log):
     return out
 
 
+def run_analysis(ref_root, log):
+    """Jackknife (src/jack.f90), get_qhat (src/gluonAna/momentum.f90),
+    Q_Average and cone_cut (src/gluonAna/gpManip.f90) on seeded inputs."""
+    tr = fortran_subset.Translator()
+    for rel in ("src/constants.f90",) + ANALYSIS_SOURCES:
+        with open(os.path.join(ref_root, rel)) as f:
+            tr.add_source(f.read())
+    ns = tr.build()
+    np.seterr(invalid="ignore")  # (ACOS of a rounding-level 1+ gives NaN, as in Fortran)
+    rng = np.random.Generator(np.random.PCG64(23))
+    data = rng.standard_normal(9) + 2.0
+    n = data.size
+    z = np.zeros(n)
+    out = {"data": data.tolist(),
+           "complement0": ns["complement0"](0.0, data)[0],
+           "complement1": ns["complement1"](n, z, data)[0].tolist(),
+           "complement2": {"icon": 3, "value": ns["complement2"](n, z, data, 3)[0].tolist()},
+           "complement3": {"icon": 2, "jcon": 7, "value": ns["complement3"](n, z, data, 2, 7)[0].tolist()}}
+    c = np.concatenate([[out["complement0"]], out["complement1"]])
+    err, bias = ns["jackknife_wp"](n, c, 0.0, 0.0)
+    out["jackknife"] = {"c": c.tolist(), "err": err, "bias": bias}
+    coords = [[0.0, 1.0, 2.0, 3.0], [3.0, -1.0, 0.0, 2.0], [1.5, 2.5, -2.0, 0.5]]
+    out["get_qhat"] = [{"coord": cd, "shape": [8, 4, 6, 4], "a": a,
+                        "qhat": ns["get_qhat"](np.array(cd), np.array([8, 4, 6, 4]), np.zeros(4), a)[0].tolist()}
+                       for cd in coords for a in (1.0, 0.7)]
+    q = np.sort(rng.uniform(0.05, 3.0, 40))
+    D = rng.uniform(0.5, 2.0, 40)
+    out["q_average"] = {"q": q.tolist(), "D": D.tolist(), "runs": []}
+    for qs in (4, 7):
+        dout, qout, qcount = ns["q_average"](40, q, D, qs, np.zeros(41), np.zeros(41), 0)
+        out["q_average"]["runs"].append({"q_slices": qs, "dout": dout.tolist(), "qout": qout.tolist(),
+                                         "qcount": int(qcount)})
+    # momenta of a 4^4 lattice (q^ of the index grid, indices above N/2 negative)
+    Q = generate_momenta((4, 4, 4, 4))
+    NQ = Q.shape[0]
+    Dq = rng.uniform(0.5, 2.0, NQ)
+    D4 = rng.uniform(0.5, 2.0, NQ)
+    out["cone_cut"] = {"lattice": [4, 4, 4, 4], "D": Dq.tolist(), "D4": D4.tolist(), "runs": []}
+    for radius, opt in ((1, (None, None, None, None)), (2, (0.6, 1.3, 1.0, 3.0)), (1, (None, 2.0, None, 0.5))):
+        qo, do, d4o, cnt = ns["cone_cut"](NQ, radius, Q, Dq, D4, 4, 4, *opt, np.zeros((NQ, 4)), np.zeros(NQ),
+                                          np.zeros(NQ), 0)
+        out["cone_cut"]["runs"].append({"radius": radius, "angle_xi_ircut_irradius": list(opt),
+                                        "qcount": int(cnt), "qout": qo[:cnt].ravel(order="F").tolist(),
+                                        "dout": do[:cnt].tolist(), "d4out": d4o[:cnt].tolist()})
+    log("  analysis helpers")
+    return out
+
+
+def generate_momenta(dims):
+    """q^_mu = 2 pi n_mu / N_mu over the index grid, n_mu > N_mu/2 taken as
+    n_mu - N_mu; rows in Fortran order of (t, x, y, z)."""
+    axes = [np.where(np.arange(n) > n // 2, np.arange(n) - n, np.arange(n)) for n in dims]
+    grid = np.stack(np.meshgrid(*axes, indexing="ij"), axis=-1).astype(np.float64)
+    q = 2.0 * np.pi * grid / np.asarray(dims, dtype=np.float64)
+    return q.transpose(3, 2, 1, 0, 4).reshape(-1, 4)
+
+
 def main(ref_root):
     tr = fortran_subset.Translator()
     for rel in SOURCES:
@@ -146,7 +206,8 @@ def main(ref_root):
                          for k in range(3)]
     alg["fixsu3matrix"] = {"in": [cplx(m) for m in fix_in],
                            "out": [cplx(ns["fixsu3matrix"](m.copy())[0]) for m in fix_in]}
-    res = {"sources": list(SOURCES), "algebra": alg, "fields": {}}
+    res = {"sources": list(SOURCES) + list(ANALYSIS_SOURCES), "algebra": alg,
+           "analysis": run_analysis(ref_root, log), "fields": {}}
     for case in CASES:
         res["fields"][case["name"]] = run_case(ns, case, log)
     with open(OUT, "w") as f:

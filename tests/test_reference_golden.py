@@ -9,6 +9,8 @@ Fortran-subset translator (`tests/golden/fortran_subset.py`, generated by
 `FixSU3Matrix` (`src/gaugeIO/ILDG_bin.f90`), on a
 random field, a Haar field and the 8^3 x 16 field of the plain-method
 benchmark case.  Every value of the C oracle must agree to FP64 rounding.
+The analysis helpers of `src/jack.f90` and `src/gluonAna/*.f90`, run the same
+way on seeded inputs, pin `flue_gb300.jack` and `flue_gb300.gluonAna`.
 """
 import json
 import os
@@ -105,3 +107,57 @@ def test_field_strength(case):
 def test_magnetic(case):
     name, U, g = case
     assert close(oracle.magnetic(U), g["magnetic"]), name
+
+
+# --- analysis helpers (src/jack.f90, src/gluonAna/momentum.f90, gpManip.f90) ---
+
+
+def test_jackknife():
+    from flue_gb300 import jack
+
+    a = GOLD["analysis"]
+    d = np.asarray(a["data"])
+    assert close(jack.complement(d), a["complement0"])
+    assert close(jack.complement(d, ("all",)), a["complement1"])
+    c2 = a["complement2"]
+    assert close(jack.complement(d, (c2["icon"] - 1,)), c2["value"])
+    c3 = a["complement3"]
+    assert close(jack.complement(d, (c3["icon"] - 1, c3["jcon"] - 1)), c3["value"])
+    err, bias = jack.jackknife_wp(a["jackknife"]["c"])
+    assert close(err, a["jackknife"]["err"]) and close(bias, a["jackknife"]["bias"])
+
+
+def test_momenta_and_qhat():
+    from flue_gb300 import gluonAna
+
+    for g in GOLD["analysis"]["get_qhat"]:
+        assert close(gluonAna.get_qhat(g["coord"], g["shape"], g["a"]), g["qhat"])
+
+
+def test_q_average():
+    from flue_gb300 import gluonAna
+
+    qa = GOLD["analysis"]["q_average"]
+    q, D = np.asarray(qa["q"]), np.asarray(qa["D"])
+    for run in qa["runs"]:
+        # the reference's DOUT is D(1) in every bin ("first")
+        dout, qout, qcount = gluonAna.q_average(q.size, q, D, run["q_slices"], stat="first")
+        assert qcount == run["qcount"]
+        assert close(qout, run["qout"]) and close(dout, run["dout"])
+
+
+def test_cone_cut():
+    from flue_gb300 import gluonAna
+
+    cc = GOLD["analysis"]["cone_cut"]
+    dims = tuple(cc["lattice"])
+    Q = gluonAna.momenta(dims).transpose(3, 2, 1, 0, 4).reshape(-1, 4)  # rows with time fastest
+    D, D4 = np.asarray(cc["D"]), np.asarray(cc["D4"])
+    names = ("angleIN", "xiIN", "IRCutIN", "IRRadiusIN")
+    for run in cc["runs"]:
+        kw = {k: v for k, v in zip(names, run["angle_xi_ircut_irradius"]) if v is not None}
+        qout, dout, d4out, qcount = gluonAna.cone_cut(Q.shape[0], run["radius"], Q, D, D4, dims[0], dims[1], **kw)
+        assert qcount == run["qcount"]
+        n = qcount
+        assert close(qout[:n].ravel(order="F"), run["qout"])
+        assert close(dout[:n], run["dout"]) and close(d4out[:n], run["d4out"])
