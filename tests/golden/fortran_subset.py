@@ -88,7 +88,7 @@ def _statements(lines: list[str]) -> list[str]:
         if cur.endswith("&"):
             cur = cur[:-1].rstrip()
             continue
-        stmts.append(cur)
+        stmts.extend(x for x in _split_top(cur, ";") if x)
         cur = ""
     return stmts
 
@@ -127,7 +127,7 @@ INTRINSICS = {
     "acos": "np.arccos", "sqrt": "np.sqrt", "exp": "np.exp", "cos": "np.cos", "sin": "np.sin",
     "sum": "_sum", "mod": "_mod", "modulo": "_modulo", "int": "_int", "dble": "float", "max": "max",
     "min": "min", "maxval": "_maxval", "minval": "_minval", "any": "_any", "count": "_count", "pack": "_pack",
-    "dot_product": "_dot", "present": "_present",
+    "dot_product": "_dot", "present": "_present", "trim": "_trim", "cshift": "_cshift",
 }
 
 
@@ -333,7 +333,69 @@ def _real(x, kind=None):
 
 
 def _cmplx(a, b=0.0, kind=None):
+    if isinstance(a, np.ndarray) or isinstance(b, np.ndarray):
+        return np.asarray(a, dtype=np.float64) + 1j * np.asarray(b, dtype=np.float64)
     return complex(a, b)
+
+
+def _trim(s):
+    return str(s).rstrip()
+
+
+def _cshift(a, shift, dim=1):
+    # CSHIFT: result(i) = a(i + shift), circularly along dimension dim
+    return np.roll(a, -int(shift), axis=int(dim) - 1)
+
+
+# --- unformatted file I/O: stream, direct (fixed-length records) and
+#     sequential (records framed by 4-byte length markers) access, big- or
+#     little-endian (the convert= specifier) ---
+class _Unit:
+    def __init__(self, path, access, recl, convert):
+        self.fh = open(path, "rb")
+        self.access = (access or "sequential").lower()
+        self.recl = int(recl) if recl is not None else 0
+        self.endian = ">" if (convert or "").lower() == "big_endian" else "<"
+        self.rec_end = None
+
+
+_ELT = {"c16": ("f8", 2), "c8": ("f4", 2), "f8": ("f8", 1), "f4": ("f4", 1), "i4": ("i4", 1), "i8": ("i8", 1)}
+
+
+def _fopen(units, unit, file=None, form=None, access=None, status=None, action=None, recl=None, convert=None):
+    units[int(unit)] = _Unit(file, access, recl, convert)
+
+
+def _fclose(units, unit):
+    units.pop(int(unit)).fh.close()
+
+
+def _frecord(units, unit, rec=None):
+    u = units[int(unit)]
+    if u.access == "direct":
+        u.fh.seek((int(rec) - 1) * u.recl)
+    elif u.access == "sequential":
+        n = int(np.frombuffer(u.fh.read(4), dtype=u.endian + "i4")[0])
+        u.rec_end = u.fh.tell() + n
+
+
+def _frecord_end(units, unit):
+    u = units[int(unit)]
+    if u.access == "sequential":
+        u.fh.seek(u.rec_end + 4)
+
+
+def _fread(units, unit, like, elt):
+    u = units[int(unit)]
+    base, per = _ELT[elt]
+    n = int(np.size(like))
+    raw = np.frombuffer(u.fh.read(n * per * int(base[1])), dtype=u.endian + base).astype(np.float64 if base[0] == "f"
+                                                                                           else np.int64)
+    vals = raw[0::2] + 1j * raw[1::2] if per == 2 else raw
+    if np.ndim(like) == 0:
+        v = vals[0]
+        return complex(v) if per == 2 else (float(v) if base[0] == "f" else int(v))
+    return vals.reshape(np.shape(like), order="F")
 
 
 def _reshape(source, shape):
@@ -685,7 +747,9 @@ class Translator:
                 continue
             dt = {"complex": "np.complex128", "real": "np.float64", "integer": "np.int64",
                   "logical": "np.bool_", "character": "object"}[d["type"]]
-            if d["dims"]:
+            if d["dims"] and any(x.strip() == ":" for x in d["dims"]):
+                L.append(f"{ind}v_{name} = None  # (allocatable: shaped by allocate)")
+            elif d["dims"]:
                 ext = []
                 for x in d["dims"]:
                     parts = _split_top(x, ":")
@@ -743,6 +807,34 @@ class Translator:
                 top = stack.pop()
                 ind = ind[:-4 * (top[1] if isinstance(top, tuple) else 1)]
                 continue
+            m = re.match(r"^select\s+case\s*\((.*)\)$", st, re.I)
+            if m:
+                n = len(stack)
+                L.append(f"{ind}_sel{n} = {self._expr(m.group(1), ctx)}")
+                stack.append(["select", n, True])
+                continue
+            m = re.match(r"^case\s*(\((.*)\)|default)$", st, re.I)
+            if m and stack and isinstance(stack[-1], list) and stack[-1][0] == "select":
+                top = stack[-1]
+                if m.group(1).lower() == "default":
+                    head = "else:"
+                else:
+                    vals = ", ".join(self._expr(v, ctx) for v in _split_top(m.group(2)))
+                    head = f"{'if' if top[2] else 'elif'} _sel{top[1]} in ({vals},):"
+                if top[2]:
+                    L.append(f"{ind}{head}")
+                    ind += "    "
+                    top[2] = False
+                else:
+                    L.append(f"{ind}pass")
+                    L.append(f"{ind[:-4]}{head}")
+                continue
+            if re.match(r"^end\s*select$", low):
+                top = stack.pop()
+                if not top[2]:
+                    L.append(f"{ind}pass")
+                    ind = ind[:-4]
+                continue
             m = re.match(r"^if\s*\((.*)\)\s*then$", st, re.I)
             if m:
                 L.append(f"{ind}if {self._expr(m.group(1), ctx)}:")
@@ -787,12 +879,63 @@ class Translator:
         self._outs[proc.name] = [proc.args.index(a) for a in outs]
         return "\n".join(L)
 
+    def _elt(self, name):
+        d = self._proc.decl.get(name, {})
+        t = d.get("type", "real")
+        return {"complex": "c16", "real": "f8", "integer": "i4"}.get(t, "f8")
+
+    def _io(self, kind, st, ctx, ind):
+        depth, j = 0, 0
+        body = st[st.index("("):]
+        for j, ch in enumerate(body):
+            depth += ch == "("
+            depth -= ch == ")"
+            if depth == 0:
+                break
+        ctl, rest = _split_top(body[1:j]), body[j + 1:].strip()
+        if kind in ("write", "deallocate"):
+            return [f"{ind}pass  # ({kind})"]
+        if kind == "allocate":
+            out = []
+            for ent in ctl:
+                nm = ent[:ent.index("(")].strip().lower()
+                dims = _split_top(ent[ent.index("(") + 1:ent.rindex(")")])
+                dt = {"complex": "np.complex128", "real": "np.float64", "integer": "np.int64"}[
+                    self._proc.decl[nm]["type"]]
+                shape = ", ".join(f"int({self._expr(x, ctx)})" for x in dims)
+                out.append(f"{ind}v_{nm} = np.zeros(({shape},), dtype={dt}, order='F')")
+            return out
+        pos = [c for c in ctl if not re.match(r"^\w+\s*=", c)]
+        kw = {c.split("=", 1)[0].strip().lower(): c.split("=", 1)[1] for c in ctl if re.match(r"^\w+\s*=", c)}
+        unit = self._expr(pos[0] if pos else kw.pop("unit"), ctx)
+        if kind == "open":
+            args = ", ".join(f"{k}={self._expr(v, ctx)}" for k, v in kw.items())
+            return [f"{ind}_fopen(_units, {unit}, {args})"]
+        if kind == "close":
+            return [f"{ind}_fclose(_units, {unit})"]
+        rec = self._expr(kw["rec"], ctx) if "rec" in kw else "None"
+        out = [f"{ind}_frecord(_units, {unit}, {rec})"]
+        for item in _split_top(rest):
+            base = (item[:item.index("(")] if "(" in item else item).strip().lower()
+            cur = self._expr(item, ctx)
+            tname, spec = self._lhs(item, ctx)
+            val = f"_fread(_units, {unit}, {cur}, '{self._elt(base)}')"
+            if spec is None:
+                out.append(f"{ind}{tname} = _assign({tname}, {val})")
+            else:
+                out.append(f"{ind}_set({tname}, ({', '.join(spec)},), {val}{self._lhs_lbs})")
+        out.append(f"{ind}_frecord_end(_units, {unit})")
+        return out
+
     def _simple(self, st, ctx, ind):
         low = st.lower()
         if low == "stop" or low.startswith("stop "):
             return [f"{ind}_stop()"]
         if low == "exit":
             return [f"{ind}break"]
+        m = re.match(r"^(open|close|read|write|allocate|deallocate)\s*\((.*)$", st, re.I)
+        if m:
+            return self._io(m.group(1).lower(), st, ctx, ind)
         if low == "cycle":
             return [f"{ind}continue"]
         if low == "return":
@@ -834,6 +977,7 @@ class Translator:
         in `only`)."""
         ns = dict(RUNTIME)
         ns["_assign"] = _assign
+        ns["_units"] = {}
         for k in ("c_double", "c_double_complex", "c_float", "c_int", "c_bool"):
             ns["v_" + k] = None
         ctx = self._ctx(None)

@@ -2,9 +2,11 @@
 
 No Fortran compiler is available, so `fortran_subset.py` translates the
 reference's `src/constants.f90`, `src/SU3MatrixOps.f90`, `src/wloops.F90`,
-the FixSU3Matrix routines of `src/gaugeIO/ILDG_bin.f90` and the analysis
-helpers (`src/jack.f90`, `src/gluonAna/momentum.f90`,
-`src/gluonAna/gpManip.f90`) statement by statement into Python over numpy (in memory) and runs the
+the gauge-file readers (`src/gaugeIO/ILDG_bin.f90`,
+`src/gaugeIO/openqcdfileio_standalone.f90`, on files written by
+`flue_gb300.gaugeIO`) and the analysis helpers (`src/jack.f90`,
+`src/gluonAna/momentum.f90`, `src/gluonAna/gpManip.f90`) statement by
+statement into Python over numpy (in memory) and runs the
 routines as written (serial build: no OpenMP / `do concurrent` macros) on the
 fields below.  Their outputs are stored in `reference_fortran.json` with the
 recipe of every input, so that the oracle (CPU) and the CUDA library (GPU)
@@ -39,8 +41,38 @@ from tests.golden import fortran_subset  # noqa: E402
 OUT = os.path.join(HERE, "reference_fortran.json")
 SOURCES = ("src/constants.f90", "src/SU3MatrixOps.f90", "src/wloops.F90", "src/gaugeIO/ILDG_bin.f90")
 ANALYSIS_SOURCES = ("src/jack.f90", "src/gluonAna/momentum.f90", "src/gluonAna/gpManip.f90")
-# file readers (Fortran I/O statements): outside the translated subset, not run
+# (the file readers are run on their own, in run_readers)
 SKIP = ("readgaugefield_ildg", "readgaugetransformation_cola")
+READER_SOURCES = ("src/gaugeIO/ILDG_bin.f90", "src/gaugeIO/openqcdfileio_standalone.f90")
+# gauge files for the readers: a 4 x 2 x 4 x 2 field (NT, NX, NY, NZ) made
+# slightly non-unitary, so that the readers' FixSU3Matrix has work to do
+READER_FIELD = {"dims": [4, 2, 4, 2], "eps": 0.3, "seed": 3, "noise": 1e-3, "noise_seed": 1, "plaq": 1.5,
+                "transform_seed": 5}
+
+
+def reader_inputs(recipe):
+    """The field and gauge transformation the reader files are written from."""
+    dims = tuple(recipe["dims"])
+    U = generate.random_field(dims, recipe["eps"], recipe["seed"])
+    rng = np.random.Generator(np.random.PCG64(recipe["noise_seed"]))
+    U = np.asfortranarray(U + recipe["noise"] * (rng.standard_normal(U.shape) + 1j * rng.standard_normal(U.shape)))
+    G = generate.random_gauge_transform(dims, recipe["transform_seed"])
+    return U, G
+
+
+def write_reader_files(recipe, d):
+    """ILDG (big-endian, direct records), openQCD (little-endian stream) and
+    cola gauge-transformation (big-endian sequential records) files written
+    by flue_gb300.gaugeIO's writers."""
+    from flue_gb300 import gaugeIO
+
+    U, G = reader_inputs(recipe)
+    paths = {"ildg": os.path.join(d, "field.ildg"), "openqcd": os.path.join(d, "field.oqcd"),
+             "cola": os.path.join(d, "transform.cola")}
+    gaugeIO.write_ildg_be(paths["ildg"], U)
+    gaugeIO.write_openqcd(paths["openqcd"], U, plaq=recipe["plaq"])
+    gaugeIO.write_gauge_transformation_cola(paths["cola"], G)
+    return paths
 
 
 def field(recipe):
@@ -169,6 +201,34 @@ def run_analysis(ref_root, log):
     return out
 
 
+def run_readers(ref_root, log):
+    """The reference's gauge-file readers on files of the three formats."""
+    import tempfile
+
+    tr = fortran_subset.Translator()
+    for rel in ("src/constants.f90",) + READER_SOURCES:
+        with open(os.path.join(ref_root, rel)) as f:
+            tr.add_source(f.read())
+    ns = tr.build()
+    nt, nx, ny, nz = READER_FIELD["dims"]
+    with tempfile.TemporaryDirectory() as d:
+        paths = write_reader_files(READER_FIELD, d)
+        out = {"recipe": READER_FIELD,
+               "ildg": field_summary7(ns["readgaugefield_ildg"](paths["ildg"], nx, ny, nz, nt)),
+               "openqcd": field_summary7(ns["readgaugefield_openqcd"](paths["openqcd"], nx, ny, nz, nt)),
+               "cola": field_summary(ns["readgaugetransformation_cola"](paths["cola"], nx, ny, nz, nt))}
+    log("  gauge-file readers")
+    return out
+
+
+def field_summary7(U):
+    """A gauge field (NT,NX,NY,NZ,4,3,3): checksum and 12 links."""
+    V = int(np.prod(U.shape[:4]))
+    flat = U.reshape((V * 4, 3, 3), order="F")
+    links = sorted({int(round(k * (4 * V - 1) / 11)) for k in range(12)})
+    return {"checksum": checksum(U), "links": {str(k): cplx(flat[k]) for k in links}}
+
+
 def generate_momenta(dims):
     """q^_mu = 2 pi n_mu / N_mu over the index grid, n_mu > N_mu/2 taken as
     n_mu - N_mu; rows in Fortran order of (t, x, y, z)."""
@@ -206,8 +266,8 @@ def main(ref_root):
                          for k in range(3)]
     alg["fixsu3matrix"] = {"in": [cplx(m) for m in fix_in],
                            "out": [cplx(ns["fixsu3matrix"](m.copy())[0]) for m in fix_in]}
-    res = {"sources": list(SOURCES) + list(ANALYSIS_SOURCES), "algebra": alg,
-           "analysis": run_analysis(ref_root, log), "fields": {}}
+    res = {"sources": list(SOURCES) + list(ANALYSIS_SOURCES) + list(READER_SOURCES), "algebra": alg,
+           "analysis": run_analysis(ref_root, log), "readers": run_readers(ref_root, log), "fields": {}}
     for case in CASES:
         res["fields"][case["name"]] = run_case(ns, case, log)
     with open(OUT, "w") as f:

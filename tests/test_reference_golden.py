@@ -10,7 +10,9 @@ Fortran-subset translator (`tests/golden/fortran_subset.py`, generated by
 random field, a Haar field and the 8^3 x 16 field of the plain-method
 benchmark case.  Every value of the C oracle must agree to FP64 rounding.
 The analysis helpers of `src/jack.f90` and `src/gluonAna/*.f90`, run the same
-way on seeded inputs, pin `flue_gb300.jack` and `flue_gb300.gluonAna`.
+way on seeded inputs, pin `flue_gb300.jack` and `flue_gb300.gluonAna`; the
+gauge-file readers of `src/gaugeIO/*.f90`, run on ILDG, openQCD and cola
+files written by `flue_gb300.gaugeIO`, pin its readers.
 """
 import json
 import os
@@ -161,3 +163,25 @@ def test_cone_cut():
         n = qcount
         assert close(qout[:n].ravel(order="F"), run["qout"])
         assert close(dout[:n], run["dout"]) and close(d4out[:n], run["d4out"])
+
+
+# --- gauge-file readers (src/gaugeIO/ILDG_bin.f90, openqcdfileio_standalone.f90) ---
+
+
+def test_gauge_file_readers(tmp_path):
+    from flue_gb300 import gaugeIO
+    from tests.golden.make_reference_golden import write_reader_files
+
+    r = GOLD["readers"]
+    nt, nx, ny, nz = r["recipe"]["dims"]
+    paths = write_reader_files(r["recipe"], str(tmp_path))
+    got = {"ildg": np.asarray(gaugeIO.read_ildg_be(paths["ildg"], nx, ny, nz, nt)),
+           "openqcd": np.asarray(gaugeIO.read_openqcd(paths["openqcd"]))}
+    for key, U in got.items():
+        want = r[key]
+        assert close(checksum(U), want["checksum"]), key
+        flat = U.reshape((-1, 3, 3), order="F")
+        for k, m in want["links"].items():
+            assert close(flat[int(k)], cx(m, (3, 3))), (key, k)
+    G = np.asarray(gaugeIO.read_gauge_transformation_cola(paths["cola"], nx, ny, nz, nt))
+    check_summary(G, r["cola"])
