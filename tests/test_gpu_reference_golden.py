@@ -11,6 +11,7 @@ import os
 
 import numpy as np
 import pytest
+import torch
 
 from flue_gb300 import gluonCalc as G
 from flue_gb300.field import GaugeField
@@ -101,3 +102,22 @@ def test_dropin_package(case):
     w = g["plaquette"]["1,4,4"]
     assert n == w["n"] and close(s, w["sum"])
     assert close(FLUE.gluonCalc.magnetic(U), g["magnetic"])
+
+
+def test_device_ingest_matches_reference_readers(tmp_path):
+    """Gauge files read straight onto the GPU (re-layout and FixSU3Matrix in
+    one kernel) equal the reference's readers run by translation."""
+    from flue_gb300 import gaugeIO
+    from tests.golden.make_reference_golden import write_reader_files
+
+    r = GOLD["readers"]
+    nt, nx, ny, nz = r["recipe"]["dims"]
+    paths = write_reader_files(r["recipe"], str(tmp_path))
+    for key, f in (("ildg", gaugeIO.read_ildg_be(paths["ildg"], nx, ny, nz, nt, device="cuda")),
+                   ("openqcd", gaugeIO.read_openqcd(paths["openqcd"], device="cuda"))):
+        U = _np(f.to_tensor(torch.complex128))
+        want = r[key]
+        assert close(checksum(U), want["checksum"]), key
+        flat = U.reshape((-1, 3, 3), order="F")
+        for k, m in want["links"].items():
+            assert close(flat[int(k)], cx(m, (3, 3))), (key, k)
