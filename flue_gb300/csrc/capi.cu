@@ -720,25 +720,31 @@ static bool cpu_writable(const void* p) {
 }
 
 // Zero-fills the listed byte ranges of host memory on up to 8 threads,
-// started at construction and joined at destruction.
+// started at construction and joined at destruction (a share whose thread
+// cannot be started is zeroed on the calling thread).
 struct HostZeroFill {
     std::vector<std::thread> th;
-    HostZeroFill(std::vector<std::pair<char*, size_t>> ranges) {
+    HostZeroFill(const std::vector<std::pair<char*, size_t>>& ranges) {
         size_t total = 0;
         for (auto& r : ranges) total += r.second;
         unsigned hw = std::thread::hardware_concurrency();
         const size_t nt = hw == 0 ? 4 : (hw < 8 ? hw : 8);
         const size_t per = (total + nt - 1) / nt;
-        // thread k zeroes bytes [k * per, (k + 1) * per) of the ranges laid end to end
+        // share k: bytes [k * per, (k + 1) * per) of the ranges laid end to end
+        auto share = [ranges, per](size_t k) {
+            size_t lo = k * per, hi = lo + per, at = 0;
+            for (auto& r : ranges) {
+                const size_t a = lo > at ? lo : at, b = hi < at + r.second ? hi : at + r.second;
+                if (a < b) memset(r.first + (a - at), 0, b - a);
+                at += r.second;
+            }
+        };
         for (size_t k = 0; k < nt && per; ++k) {
-            th.emplace_back([ranges, per, k] {
-                size_t lo = k * per, hi = lo + per, at = 0;
-                for (auto& r : ranges) {
-                    const size_t a = lo > at ? lo : at, b = hi < at + r.second ? hi : at + r.second;
-                    if (a < b) memset(r.first + (a - at), 0, b - a);
-                    at += r.second;
-                }
-            });
+            try {
+                th.emplace_back(share, k);
+            } catch (...) {
+                share(k);
+            }
         }
     }
     ~HostZeroFill() {
