@@ -5,7 +5,9 @@ array constructors and RESHAPE, integer division, do loops with steps and
 empty ranges, block / one-line if with else-if, do concurrent, subroutine
 calls with copy-out of intent(out) / intent(inout) arguments (whole
 variables, elements and sections), functions returning arrays, complex
-literals and kinds, parameters, and the preprocessor's serial branch."""
+literals and kinds, parameters, and the preprocessor's serial branch; and
+its emulation of unformatted I/O (stream, direct and sequential access,
+either byte order)."""
 import numpy as np
 
 from tests.golden import fortran_subset as fs
@@ -120,3 +122,57 @@ def test_translated_module_runs_as_fortran():
     # section arguments copied out: m(1, 2:3) = [3, 5] doubled into sec(2:3)
     assert list(sec) == [0.0, 6.0, 10.0, 7.0]
     assert conc == sum(a * b for a in (1, 2) for b in (1, 2, 3))
+
+
+IO_SRC = """
+module m_io
+   implicit none
+contains
+   subroutine read_all(fstream, fdirect, fseq, n, ivals, x, rec2, seq2)
+      character(len=*), intent(in) :: fstream, fdirect, fseq
+      integer, intent(in) :: n
+      integer, dimension(2), intent(out) :: ivals
+      real(kind=8), intent(out) :: x
+      complex(kind=8), dimension(n), intent(out) :: rec2
+      real(kind=8), dimension(n, 2), intent(out) :: seq2
+      integer :: k
+      open (11, file=TRIM(fstream), form='unformatted', access='stream', status='old', convert='little_endian')
+      read (11) ivals(1), ivals(2), x
+      close (11)
+      open (12, file=fdirect, form='unformatted', access='direct', recl=16 * n, convert='BIG_ENDIAN')
+      read (12, rec=2) rec2
+      close (12)
+      open (13, file=fseq, form='unformatted', status='old', convert='BIG_ENDIAN')
+      do k = 1, 2
+         read (13) seq2(:, k)
+      end do
+      close (13)
+   end subroutine read_all
+end module m_io
+"""
+
+
+def test_translated_unformatted_io(tmp_path):
+    """Stream (little-endian, mixed integer / real items), direct (big-endian
+    fixed-length records, the second one read) and sequential (big-endian
+    records framed by 4-byte lengths) access."""
+    n = 3
+    fs_ = tmp_path / "s.bin"
+    fs_.write_bytes(np.array([7, -2], "<i4").tobytes() + np.array([2.5], "<f8").tobytes())
+    fd = tmp_path / "d.bin"
+    recs = np.arange(2 * n, dtype=np.float64).reshape(2, n) + 1j * 10
+    fd.write_bytes(recs.astype(">c16").tobytes())
+    fq = tmp_path / "q.bin"
+    cols = [np.array([1.0, 2.0, 3.0]), np.array([4.0, 5.0, 6.0])]
+    with open(fq, "wb") as fh:
+        for c in cols:
+            m = np.array([c.nbytes], ">i4").tobytes()
+            fh.write(m + c.astype(">f8").tobytes() + m)
+    tr = fs.Translator()
+    tr.add_source(IO_SRC)
+    ns = tr.build()
+    ivals, x, rec2, seq2 = ns["read_all"](str(fs_), str(fd), str(fq), n, np.zeros(2, np.int64), 0.0,
+                                          np.zeros(n, np.complex128), np.zeros((n, 2)))
+    assert list(ivals) == [7, -2] and x == 2.5
+    assert np.array_equal(rec2, recs[1])
+    assert np.array_equal(seq2[:, 0], cols[0]) and np.array_equal(seq2[:, 1], cols[1])
