@@ -109,10 +109,13 @@ CASES = [
     {"name": "random_4x3x4x3", "recipe": {"kind": "random", "dims": [4, 3, 4, 3], "eps": 0.4, "seed": 5},
      "full": True},
     {"name": "haar_3x4x2x3", "recipe": {"kind": "haar", "dims": [3, 4, 2, 3], "seed": 7}, "full": True},
+    {"name": "strong_5x2x3x4", "recipe": {"kind": "random", "dims": [5, 2, 3, 4], "eps": 0.9, "seed": 17},
+     "full": True},
+    {"name": "haar_2x3x3x2", "recipe": {"kind": "haar", "dims": [2, 3, 3, 2], "seed": 19}, "full": True},
     {"name": "config0_8x8x8x16", "recipe": {"kind": "random", "dims": [16, 8, 8, 8], "eps": 0.3, "seed": 1},
      "full": False},
 ]
-# (coordinates inside every lattice below: t, x, z <= 3, y <= 2)
+# (coordinates taken modulo each lattice's extents)
 PATHS = [
     ([1, 1, 1, 1], [1, 2, -1, -2]),
     ([2, 3, 1, 2], [2, 3, -2, -3, 4, 4, -4, -4]),
@@ -135,10 +138,14 @@ def run_case(ns, case, log):
         sg, ng, _ = ns["genplaquette"](U, NT, NX, NY, NZ, *rng, 0.0, 0, 0.0)
         plaq[",".join(map(str, rng))] = {"sum": s, "n": int(n), "gen_sum": sg, "gen_n": int(ng)}
     out["plaquette"] = plaq
-    s, n, _ = ns["polyakov"](U, 0.0, 0, 0.0)
-    out["polyakov"] = {"sum": s, "n": int(n)}
-    out["genericpath"] = [{"coord": c, "path": p, "matrix": cplx(ns["genericpath"](U, np.array(c), np.array(p)))}
-                          for c, p in PATHS]
+    if NT >= 3:  # (the reference's loop leaves its product undefined for NT < 3)
+        s, n, _ = ns["polyakov"](U, 0.0, 0, 0.0)
+        out["polyakov"] = {"sum": s, "n": int(n)}
+    out["genericpath"] = []
+    for c, p in PATHS:
+        c = [(ci - 1) % n + 1 for ci, n in zip(c, (NT, NX, NY, NZ))]
+        out["genericpath"].append({"coord": c, "path": p,
+                                   "matrix": cplx(ns["genericpath"](U, np.array(c), np.array(p)))})
     out["wmunu"] = [{"args": list(a), "value": ns["wmunu"](U, *a)} for a in WLOOPS]
     out["wmunutau"] = [{"args": list(a), "value": ns["wmunutau"](U, *a)} for a in WLOOPS_TAU]
     log(f"  {case['name']}: plaquette, polyakov, paths, loops {time.time() - t:.1f} s")

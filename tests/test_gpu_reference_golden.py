@@ -65,8 +65,9 @@ def test_observables(case):
         r = tuple(int(v) for v in rng.split(","))
         s, n, _ = G.plaquette(f, *r)
         assert n == w["n"] and close(s, w["sum"]), (name, rng)
-    s, n, _ = G.polyakov(f)
-    assert n == g["polyakov"]["n"] and close(s, g["polyakov"]["sum"]), name
+    if "polyakov" in g:  # (NT >= 3: the reference leaves NT < 3 undefined)
+        s, n, _ = G.polyakov(f)
+        assert n == g["polyakov"]["n"] and close(s, g["polyakov"]["sum"]), name
     for p in g["genericpath"]:
         assert close(_np(G.genericpath(f, p["coord"], p["path"])), cx(p["matrix"], (3, 3))), (name, p["path"])
     for w in g["wmunu"]:

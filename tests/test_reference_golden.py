@@ -80,6 +80,8 @@ def test_plaquettes(case):
 
 def test_polyakov(case):
     name, U, g = case
+    if "polyakov" not in g:
+        pytest.skip("the reference defines the Polyakov loop for NT >= 3 only")
     s, n = oracle.polyakov(U)
     assert n == g["polyakov"]["n"] and close(s, g["polyakov"]["sum"]), name
 
