@@ -852,7 +852,10 @@ int magnetic_force_pipelined(DevCache* c, const void* d_in, const void* h_in, vo
     // The first pack and the last write-out have no compute beside them and
     // run on the whole GPU (8 slabs: 11.95 -> 11.79 ms per call).
     const unsigned in_blocks = (unsigned)env_int("FLUE_IN_BLOCKS", 32);
-    const unsigned out_blocks = (unsigned)env_int("FLUE_OUT_BLOCKS", 16);
+    // (with the time direction off the link, same box, median per call: a
+    // complex128 field 9.68 ms with 16 x 4 output blocks, 9.53 with 12 x 4;
+    // complex64 9.09 with 16, 9.12 with 12)
+    const unsigned out_blocks = (unsigned)env_int("FLUE_OUT_BLOCKS", esz == 16 ? 12 : 16);
     // B^2 has no plane with the time direction: its links are not packed
     // (pmu0 = 1) and its gradient is zero.  With the gradient in host memory
     // the CPU writes those zeros while the GPU computes, so that only the
